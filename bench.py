@@ -1,0 +1,390 @@
+"""Benchmark: committed field elements per second for the Ligerito / RS commit
+(additive NTT + Merkle, bit-exact) of a 2^24-element polynomial laid out as a
+2^12 x 2^12 matrix, rate 1/4, BLAKE3 Merkle tree over 16384 columns.
+
+  python bench.py [--gpus N] [--steps K] [--warmup W] [--impl gb300|reference]
+
+One JSON line on stdout (rank 0).  Under torchrun each rank commits its own
+polynomial (independent objects, no data-path collective: weak scaling); the
+timed region is bracketed by a barrier and a device synchronize, and the
+maximum over ranks is reported.  The reference arm times the CPU
+restatement of the reference's commit (oracle/, "port": the reference is Rust
+and no Rust toolchain exists on the machine) on all host cores.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+REPO = os.path.dirname(os.path.abspath(__file__))
+for _p in (REPO, os.path.join(REPO, "bitz-poc_gb300")):
+    if _p not in sys.path:
+        sys.path.insert(0, _p)
+
+LOG_N = 24          # 2^24 committed GF(2^128) elements
+LOG_LANES = 12      # 2^12 matrix rows (interleaved lanes) x 2^12 columns
+LOG_INV_RATE = 2    # rate 1/4 -> 16384 codeword columns (Merkle leaves)
+HASH = 1            # BLAKE3
+SEED = 1
+METRIC = "committed field elems/sec (NTT+Merkle, bit-exact) at 2^24"
+UNIT = "elems/s"
+WORKLOAD = {
+    "workload": "ligerito_rs_commit_2^24",
+    "matrix": "2^12 x 2^12 GF(2^128)",
+    "rate": "1/4",
+    "merkle_leaves": 16384,
+    "hash": "blake3",
+    "inputs": "ChaCha20 seed 1 (+rank), uniform GF(2^128)",
+    "l2": "inputs larger than L2: 256 MiB message, 1 GiB codeword per step",
+}
+MSG_BYTES = 16 << LOG_N
+ALG_BYTES_PER_WORD = 16 + (16 << LOG_INV_RATE)   # read message + write codeword
+
+
+def _dist():
+    ws = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return ws, rank, local
+
+
+class _Dist:
+    def __init__(self, ws, local):
+        self.ws = ws
+        self.pg = None
+        if ws > 1:
+            import torch
+            import torch.distributed as dist
+
+            backend = "nccl" if torch.cuda.is_available() else "gloo"
+            if backend == "nccl":
+                torch.cuda.set_device(local)
+            dist.init_process_group(backend)
+            self.dist = dist
+            self.torch = torch
+            self.dev = torch.device("cuda", local) if backend == "nccl" else torch.device("cpu")
+
+    def barrier(self):
+        if self.ws > 1:
+            self.dist.barrier()
+
+    def max(self, x: float) -> float:
+        if self.ws == 1:
+            return x
+        t = self.torch.tensor([x], dtype=self.torch.float64, device=self.dev)
+        self.dist.all_reduce(t, op=self.dist.ReduceOp.MAX)
+        return float(t.item())
+
+    def close(self):
+        if self.ws > 1:
+            self.dist.destroy_process_group()
+
+
+class _Clocks:
+    """nvidia-smi samples during the timed region."""
+
+    def __init__(self, index: int):
+        self.index = index
+        self.proc = None
+        self.lines = []
+
+    def start(self):
+        q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+             "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+             "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", f"--id={self.index}", f"--query-gpu={q}", "--format=csv,noheader,nounits",
+                 "-lms", "100"], stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            threading.Thread(target=self._read, daemon=True).start()
+        except OSError:
+            self.proc = None
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def stop(self):
+        if self.proc:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+        sm, mx, reasons = [], 0.0, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            f = [x.strip() for x in ln.split(",")]
+            if len(f) < 9:
+                continue
+            try:
+                sm.append(float(f[1]))
+                mx = max(mx, float(f[2]))
+            except ValueError:
+                continue
+            for n, v in zip(names, f[5:9]):
+                if v.lower().startswith("active"):
+                    reasons.add(n)
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": mx or None,
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def _peaks():
+    try:
+        with open(os.path.join(REPO, "MEASURED_PEAKS.json")) as fh:
+            d = json.load(fh)
+        return float(d["hbm_gbs"]), "measured"
+    except (OSError, KeyError, ValueError):
+        return 6800.0, "fallback"
+
+
+def cpu_baseline(n_threads: int, log_n: int = LOG_N):
+    """The oracle commit (CPU restatement of the reference) on a full 2^24
+    commit with all host threads; elements per second."""
+    from oracle import oracle as O
+
+    O.build()
+    msg = O.chacha_words(SEED, 1 << log_n)
+    t0 = time.perf_counter()
+    _, _, root = O.commit(msg, LOG_INV_RATE, LOG_LANES, HASH, n_threads=n_threads)
+    dt = time.perf_counter() - t0
+    return (1 << log_n) / dt, dt, root
+
+
+def run_reference(args, ws, rank):
+    if rank != 0:
+        return 0
+    from oracle import oracle as O
+
+    O.build()
+    threads = os.cpu_count() or 1
+    msg = O.chacha_words(SEED, 1 << LOG_N)
+    times = []
+    for i in range(args.warmup + args.steps):
+        t0 = time.perf_counter()
+        O.commit(msg, LOG_INV_RATE, LOG_LANES, HASH, n_threads=threads)
+        dt = time.perf_counter() - t0
+        if i >= args.warmup:
+            times.append(dt)
+    total = sum(times)
+    value = args.steps * (1 << LOG_N) / total
+    line = {
+        "impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": ws,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * total / args.steps,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "u64 (GF(2^128))",
+        "data": "synthetic", "config": dict(WORKLOAD, parallelism=f"replicas{ws}"),
+        "cpu_baseline": {"value": value, "unit": UNIT, "cores": threads, "kind": "port",
+                         "sample": "full 2^24-element commit per step (CPU restatement of the "
+                                   "reference, all host threads); no Rust toolchain for the "
+                                   "reference's own rayon path"},
+        "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line), flush=True)
+    return 0
+
+
+def run_gpu(args, ws, rank, local):
+    import numpy as np
+
+    import bitz_gb300 as bz
+    from bitz_gb300 import _lib
+
+    D = _Dist(ws, local)
+    ctx = bz.Context(local)
+    L = _lib.lib()
+    params = bz.PcsParams(LOG_N + 7, LOG_INV_RATE, LOG_LANES, HASH)
+    pc = params.to_c()
+    import ctypes
+
+    msg = bz.DeviceArray.chacha(SEED + rank, 1 << LOG_N, ctx)
+
+    def one_commit():
+        h = ctypes.c_void_p()
+        _lib.check(ctx.handle, L.bz_commit_device_async(ctx.handle, msg.ptr, 1 << LOG_N,
+                                                        ctypes.byref(pc), ctypes.byref(h)))
+        root = (ctypes.c_uint8 * 32)()
+        _lib.check(ctx.handle, L.bz_commitment_root(h, root))
+        L.bz_commitment_free(h)
+        return bytes(root)
+
+    # parity of the benchmarked output against the committed oracle root
+    root0 = one_commit()
+    with open(os.path.join(REPO, "tests", "golden", "roots.json")) as fh:
+        golden = {(e["log_msg_len"], e["seed"], e["hash"]): e["root"]
+                  for e in json.load(fh)["roots"]}
+    exp = golden.get((LOG_N, SEED + rank, "blake3"))
+    parity = None if exp is None else (root0.hex() == exp)
+    if parity is False:
+        raise SystemExit(f"benchmarked commit root {root0.hex()} != oracle root {exp}")
+
+    for _ in range(max(args.warmup, 3) - 1):
+        one_commit()
+
+    # ---- device-resident timed region -----------------------------------
+    launches0 = ctx.kernel_launches()
+    clocks = _Clocks(local)
+    D.barrier()
+    ctx.synchronize()
+    clocks.start()
+    step_ms = []
+    ctx.timer_begin()
+    t_all0 = time.perf_counter()
+    for _ in range(args.steps):
+        ctx.timer_begin()
+        one_commit()
+        step_ms.append(ctx.timer_end())
+    ctx.synchronize()
+    wall = time.perf_counter() - t_all0
+    D.barrier()
+    clk = clocks.stop()
+    launches = ctx.kernel_launches() - launches0
+    total_ms = sum(step_ms)
+    total_ms = D.max(total_ms)
+    value = ws * args.steps * (1 << LOG_N) / (total_ms / 1e3)
+
+    # ---- end to end through the C ABI with host buffers ----------------
+    hp = ctypes.c_void_p()
+    _lib.check(None, L.bz_host_alloc_pinned(MSG_BYTES, ctypes.byref(hp)))
+    _lib.check(None, L.bz_chacha_fill_host(SEED + rank, 0, hp, 1 << LOG_N, os.cpu_count() or 1))
+
+    def e2e_commit():
+        h = ctypes.c_void_p()
+        root = (ctypes.c_uint8 * 32)()
+        _lib.check(ctx.handle, L.bz_commit(ctx.handle, hp, 1 << LOG_N, ctypes.byref(pc),
+                                           ctypes.byref(h), root))
+        L.bz_commitment_free(h)
+        return bytes(root)
+
+    assert e2e_commit() == root0
+    e2e_commit()
+    D.barrier()
+    ctx.synchronize()
+    ctx.timer_begin()
+    for _ in range(args.steps):
+        e2e_commit()
+    e2e_ms = D.max(ctx.timer_end())
+    e2e_value = ws * args.steps * (1 << LOG_N) / (e2e_ms / 1e3)
+    L.bz_host_free_pinned(hp)
+
+    out = None
+    if rank == 0:
+        # ---- per-kernel phase times and the roofline of the dominant kernel
+        phases, proot = ctx.commit_profile(msg, params)
+        assert proot == root0
+        agg = {}
+        for name, ms in phases:
+            a = agg.setdefault(name, [0, 0.0])
+            a[0] += 1
+            a[1] += ms
+        total_phase = sum(v[1] for v in agg.values())
+        dom = max(agg.items(), key=lambda kv: kv[1][1])
+        dom_name, (dom_n, dom_ms) = dom
+        cw_bytes = 16 << (LOG_N + LOG_INV_RATE)
+        # per launch: an in-place table pass reads and writes the codeword once
+        if dom_name.endswith("_first"):
+            alg_bytes = MSG_BYTES + cw_bytes
+        elif dom_name.startswith("ntt"):
+            alg_bytes = 2 * cw_bytes
+        else:
+            alg_bytes = cw_bytes
+        peak, peak_kind = _peaks()
+        achieved = alg_bytes / (dom_ms / dom_n / 1e3) / 1e9
+        commit_ms = statistics.median(step_ms)
+        commit_gbs = ALG_BYTES_PER_WORD * (1 << LOG_N) / (commit_ms / 1e3) / 1e9
+
+        # ---- batched (64 polys, log2 sizes U[16, 24], seed 3) vs plain -----
+        batch = None
+        if not args.skip_batch:
+            batch = _bench_batch(ctx, bz, L, _lib, args)
+
+        # ---- CPU baseline (oracle, all host threads, one full commit) -----
+        cpu = None
+        if not args.skip_cpu:
+            threads = os.cpu_count() or 1
+            v, dt, croot = cpu_baseline(threads)
+            assert croot == root0 or rank != 0 or SEED + rank != SEED
+            cpu = {"value": v, "unit": UNIT, "cores": threads, "kind": "port",
+                   "sample": f"one full 2^24-element commit ({dt:.2f} s) by the CPU "
+                             "restatement of the reference on all host threads"}
+        sorted_ms = sorted(step_ms)
+        p99 = sorted_ms[min(len(sorted_ms) - 1, int(round(0.99 * (len(sorted_ms) - 1))))]
+        out = {
+            "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": ws, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": total_ms / args.steps,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+            "dtype": "u64 (GF(2^128) carry-less)", "data": "synthetic",
+            "config": dict(WORKLOAD, parallelism=f"replicas{ws}"),
+            "parity": {"root_matches_oracle": parity, "root": root0.hex()},
+            "latency_ms": {"p50": statistics.median(step_ms), "p99": p99,
+                           "min": sorted_ms[0], "max": sorted_ms[-1]},
+            "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": MSG_BYTES,
+                    "d2h_bytes_per_step": 32},
+            "roofline": {"bound": "hbm", "kernel": dom_name, "achieved": achieved, "peak": peak,
+                         "unit": "GB/s", "frac": achieved / peak, "traffic": None,
+                         "alg_bytes_per_launch": alg_bytes, "launch_ms": dom_ms / dom_n,
+                         "peak_source": peak_kind,
+                         "commit_alg_gbs": commit_gbs, "commit_frac": commit_gbs / peak},
+            "phases_ms": {k: round(v[1], 4) for k, v in agg.items()},
+            "phase_share": {k: round(v[1] / total_phase, 4) for k, v in agg.items()},
+            "clocks": clk, "gpu_launches": launches, "wall_s": wall,
+            "batched": batch, "cpu_baseline": cpu,
+        }
+        print(json.dumps(out), flush=True)
+    msg.free()
+    ctx.close()
+    D.close()
+    return 0
+
+
+def _bench_batch(ctx, bz, L, _lib, args):
+    import numpy as np
+
+    rng = np.random.default_rng(3)
+    sizes = rng.integers(16, 25, 64)
+    params = [bz.PcsParams(int(n) + 7, LOG_INV_RATE, int(n) // 2, HASH) for n in sizes]
+    msgs = [bz.DeviceArray.chacha(3000 + i, 1 << int(n), ctx) for i, n in enumerate(sizes)]
+    total = int(sum(1 << int(n) for n in sizes))
+    res = {}
+    for mode, graph in (("graph", True), ("plain", False)):
+        out = bz.commit_batch(msgs, params, use_graph=graph, ctx=ctx)  # warm-up
+        for _, pd in out:
+            pd.free()
+        ctx.synchronize()
+        t0 = time.perf_counter()
+        reps = 3
+        for _ in range(reps):
+            out = bz.commit_batch(msgs, params, use_graph=graph, ctx=ctx)
+            for _, pd in out:
+                pd.free()
+        ctx.synchronize()
+        dt = (time.perf_counter() - t0) / reps
+        res[mode] = {"value": total / dt, "ms": dt * 1e3}
+    for m in msgs:
+        m.free()
+    return {"polys": 64, "total_elems": total, "unit": UNIT,
+            "log2_sizes": [int(x) for x in sizes], **res}
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=10)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
+    ap.add_argument("--skip-cpu", action="store_true")
+    ap.add_argument("--skip-batch", action="store_true")
+    args = ap.parse_args()
+    ws, rank, local = _dist()
+    if args.impl == "reference":
+        return run_reference(args, ws, rank)
+    return run_gpu(args, ws, rank, local)
+
+
+if __name__ == "__main__":
+    sys.exit(main())

@@ -1,0 +1,22 @@
+"""GB300-native Ligerito / Reed-Solomon commitment path of BitZ.
+
+The compute path is libbitzgpu.so (hand-written sm_103a CUDA behind the C ABI
+in include/bitz_gpu.h); this package is the host-side mirror of the
+reference's commit/open interface over that ABI.
+"""
+from ._lib import BzError, declared_symbols, lib, lib_path  # noqa: F401
+from .pcs import (  # noqa: F401
+    LOG_PACKING,
+    Commitment,
+    Context,
+    DeviceArray,
+    HashKind,
+    LigeroWitness,
+    PcsParams,
+    ProverData,
+    chacha_words,
+    commit,
+    commit_batch,
+    default_context,
+    ligero_commit,
+)

@@ -1,0 +1,240 @@
+// Batched commits captured into one CUDA graph, the NTT schedule autotuner
+// and the host-side ChaCha20 input generator.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cstring>
+#include <thread>
+#include <vector>
+
+#include "runtime.h"
+
+using namespace bz;
+
+namespace {
+
+// RFC 8439 block function (host).
+inline uint32_t rotl32(uint32_t x, int n) { return (x << n) | (x >> (32 - n)); }
+void chacha_block(uint32_t k0, uint32_t k1, uint32_t counter, uint32_t out[16]) {
+    uint32_t st[16] = {0x61707865u, 0x3320646eu, 0x79622d32u, 0x6b206574u, k0, k1, 0, 0,
+                       0, 0, 0, 0, counter, 0, 0, 0};
+    uint32_t x[16];
+    memcpy(x, st, sizeof x);
+    auto qr = [&](int a, int b, int c, int d) {
+        x[a] += x[b]; x[d] = rotl32(x[d] ^ x[a], 16);
+        x[c] += x[d]; x[b] = rotl32(x[b] ^ x[c], 12);
+        x[a] += x[b]; x[d] = rotl32(x[d] ^ x[a], 8);
+        x[c] += x[d]; x[b] = rotl32(x[b] ^ x[c], 7);
+    };
+    for (int i = 0; i < 10; ++i) {
+        qr(0, 4, 8, 12); qr(1, 5, 9, 13); qr(2, 6, 10, 14); qr(3, 7, 11, 15);
+        qr(0, 5, 10, 15); qr(1, 6, 11, 12); qr(2, 7, 8, 13); qr(3, 4, 9, 14);
+    }
+    for (int i = 0; i < 16; ++i) out[i] = x[i] + st[i];
+}
+
+void chacha_range(uint64_t seed, uint64_t first_word, uint64_t *out, size_t lo, size_t hi) {
+    const uint32_t k0 = (uint32_t)seed, k1 = (uint32_t)(seed >> 32);
+    uint32_t blk[16];
+    uint64_t cached = ~0ull;
+    for (size_t i = lo; i < hi; ++i) {
+        const uint64_t w = first_word + i, b = w >> 2;
+        if (b != cached) {
+            chacha_block(k0, k1, (uint32_t)b, blk);
+            cached = b;
+        }
+        const uint32_t *p = blk + 4 * (w & 3);
+        out[2 * i] = (uint64_t)p[0] | ((uint64_t)p[1] << 32);
+        out[2 * i + 1] = (uint64_t)p[2] | ((uint64_t)p[3] << 32);
+    }
+}
+
+}  // namespace
+
+extern "C" {
+
+int bz_chacha_fill_host(uint64_t seed, uint64_t first_word, uint64_t *out, size_t n_words,
+                        int n_threads) {
+    if (n_words && !out) return BZ_ERR_ARG;
+    if (n_threads < 1) n_threads = 1;
+    if (n_threads == 1 || n_words < (1u << 16)) {
+        chacha_range(seed, first_word, out, 0, n_words);
+        return BZ_OK;
+    }
+    std::vector<std::thread> th;
+    const size_t per = ((n_words + n_threads - 1) / n_threads + 3) & ~(size_t)3;
+    for (int t = 0; t < n_threads; ++t) {
+        const size_t lo = (size_t)t * per, hi = std::min(n_words, lo + per);
+        if (lo >= hi) break;
+        th.emplace_back(chacha_range, seed, first_word, out, lo, hi);
+    }
+    for (auto &t : th) t.join();
+    return BZ_OK;
+}
+
+// ---- batched commit -------------------------------------------------------
+int bz_commit_batch_device(bz_ctx *ctx, size_t count, const uint64_t *const *d_msgs,
+                           const bz_params *params, bz_commitment **outs, uint8_t *roots,
+                           int use_graph) {
+    if (!ctx || !d_msgs || !params || !outs) return BZ_ERR_ARG;
+    std::vector<Shape> shapes(count);
+    for (size_t i = 0; i < count; ++i) {
+        outs[i] = nullptr;
+        std::string why;
+        if (!d_msgs[i]) return set_msg(ctx, BZ_ERR_ARG, "null message");
+        int rc = shape_from_params(&params[i], shapes[i],
+                                   (size_t)1 << params[i].log_msg_len, why);
+        if (rc) return set_msg(ctx, rc, why);
+    }
+    // Resident buffers, twiddles and scratch are set up before any capture.
+    size_t scratch = 0;
+    for (size_t i = 0; i < count; ++i) {
+        const uint4 *tw = nullptr;
+        int rc = get_twiddles(ctx, shapes[i].k_code(), &tw);
+        if (rc) return rc;
+        scratch = std::max(scratch, merkle_scratch_bytes(shapes[i]));
+        rc = alloc_commitment(ctx, shapes[i], &outs[i]);
+        if (rc) {
+            for (size_t j = 0; j < i; ++j) {
+                bz_commitment_free(outs[j]);
+                outs[j] = nullptr;
+            }
+            return rc;
+        }
+    }
+    if (scratch) {
+        int rc = ensure_scratch(ctx, scratch);
+        if (rc) return rc;
+    }
+    void *d_roots = nullptr;
+    int rc = dev_alloc(ctx, count * 32, &d_roots, false);
+    if (rc) return rc;
+    cudaStream_t st = ctx->stream;
+    cudaGraph_t graph = nullptr;
+    cudaGraphExec_t exec = nullptr;
+    if (use_graph) {
+        cudaError_t e = cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal);
+        if (e != cudaSuccess) return set_err(ctx, BZ_ERR_CUDA, "begin capture", e);
+    }
+    for (size_t i = 0; i < count && rc == BZ_OK; ++i) {
+        rc = enqueue_commit(ctx, shapes[i], (const uint4 *)d_msgs[i], outs[i], st,
+                            schedule_for(ctx, shapes[i]));
+        if (rc == BZ_OK) {
+            const uint8_t *src = outs[i]->d_tree + (shapes[i].tree_nodes() - 1) * 32;
+            cudaMemcpyAsync((uint8_t *)d_roots + 32 * i, src, 32, cudaMemcpyDeviceToDevice, st);
+        }
+    }
+    if (use_graph) {
+        cudaError_t e = cudaStreamEndCapture(st, &graph);
+        if (rc == BZ_OK && e != cudaSuccess) rc = set_err(ctx, BZ_ERR_CUDA, "end capture", e);
+        if (rc == BZ_OK) {
+            e = cudaGraphInstantiate(&exec, graph, 0);
+            if (e != cudaSuccess) rc = set_err(ctx, BZ_ERR_CUDA, "instantiate", e);
+        }
+        if (rc == BZ_OK) {
+            e = cudaGraphLaunch(exec, st);
+            if (e != cudaSuccess) rc = set_err(ctx, BZ_ERR_CUDA, "graph launch", e);
+        }
+    }
+    if (rc == BZ_OK && roots) {
+        cudaMemcpyAsync(roots, d_roots, count * 32, cudaMemcpyDeviceToHost, st);
+    }
+    cudaError_t e = cudaStreamSynchronize(st);
+    if (rc == BZ_OK && e != cudaSuccess) rc = set_err(ctx, BZ_ERR_CUDA, "batch sync", e);
+    if (exec) cudaGraphExecDestroy(exec);
+    if (graph) cudaGraphDestroy(graph);
+    dev_free(ctx, d_roots, 0, false);
+    if (rc == BZ_OK && roots) {
+        for (size_t i = 0; i < count; ++i) {
+            memcpy(outs[i]->root, roots + 32 * i, 32);
+            outs[i]->root_ready = true;
+        }
+    }
+    if (rc != BZ_OK) {
+        for (size_t i = 0; i < count; ++i) {
+            if (outs[i]) bz_commitment_free(outs[i]);
+            outs[i] = nullptr;
+        }
+    }
+    return rc;
+}
+
+// ---- schedules ------------------------------------------------------------
+int bz_schedule_get(bz_ctx *ctx, const bz_params *params, uint32_t *schedule) {
+    if (!ctx || !params || !schedule) return BZ_ERR_ARG;
+    Shape s;
+    std::string why;
+    int rc = shape_from_params(params, s, (size_t)1 << params->log_msg_len, why);
+    if (rc) return set_msg(ctx, rc, why);
+    *schedule = schedule_for(ctx, s);
+    return BZ_OK;
+}
+
+int bz_schedule_set(bz_ctx *ctx, const bz_params *params, uint32_t schedule) {
+    if (!ctx || !params) return BZ_ERR_ARG;
+    Shape s;
+    std::string why;
+    int rc = shape_from_params(params, s, (size_t)1 << params->log_msg_len, why);
+    if (rc) return set_msg(ctx, rc, why);
+    std::lock_guard<std::mutex> g(ctx->sched_mu);
+    ctx->schedules[shape_key(s)] = schedule;
+    return BZ_OK;
+}
+
+int bz_autotune(bz_ctx *ctx, const bz_params *params, int reps, uint32_t *chosen) {
+    if (!ctx || !params) return BZ_ERR_ARG;
+    Shape s;
+    std::string why;
+    int rc = shape_from_params(params, s, (size_t)1 << params->log_msg_len, why);
+    if (rc) return set_msg(ctx, rc, why);
+    if (reps < 1) reps = 1;
+    void *d_msg = nullptr;
+    rc = dev_alloc(ctx, s.msg_words() * 16, &d_msg, false);
+    if (rc) return rc;
+    bz_chacha_fill_device(ctx, 12345, 0, (uint64_t *)d_msg, s.msg_words());
+    bz_commitment *c = nullptr;
+    rc = alloc_commitment(ctx, s, &c);
+    if (rc) {
+        dev_free(ctx, d_msg, 0, false);
+        return rc;
+    }
+    std::vector<uint32_t> cands;
+    const int b = s.log_dim();
+    for (int d = 0; d <= std::min(4, b); ++d) {
+        cands.push_back((uint32_t)d);
+        cands.push_back((uint32_t)d | SCHED_RADIX2);
+    }
+    float best = 1e30f;
+    uint32_t best_s = default_schedule(s);
+    for (uint32_t cand : cands) {
+        // warm-up, then timed reps
+        rc = enqueue_commit(ctx, s, (const uint4 *)d_msg, c, ctx->stream, cand);
+        if (rc) break;
+        cudaEventRecord(ctx->ev0, ctx->stream);
+        for (int r = 0; r < reps && rc == BZ_OK; ++r)
+            rc = enqueue_commit(ctx, s, (const uint4 *)d_msg, c, ctx->stream, cand);
+        cudaEventRecord(ctx->ev1, ctx->stream);
+        if (cudaEventSynchronize(ctx->ev1) != cudaSuccess) {
+            rc = set_msg(ctx, BZ_ERR_CUDA, "autotune sync");
+            break;
+        }
+        float ms = 0;
+        cudaEventElapsedTime(&ms, ctx->ev0, ctx->ev1);
+        if (ms < best) {
+            best = ms;
+            best_s = cand;
+        }
+    }
+    bz_commitment_free(c);
+    dev_free(ctx, d_msg, 0, false);
+    cudaStreamSynchronize(ctx->stream);
+    if (rc) return rc;
+    {
+        std::lock_guard<std::mutex> g(ctx->sched_mu);
+        ctx->schedules[shape_key(s)] = best_s;
+    }
+    if (chosen) *chosen = best_s;
+    return BZ_OK;
+}
+
+}  // extern "C"

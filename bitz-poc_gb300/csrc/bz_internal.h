@@ -1,0 +1,101 @@
+// Internal interfaces between the CUDA translation units and the host
+// runtime (context, commit pipeline, batching, serving).  Not part of the ABI.
+#pragma once
+#include <cuda_runtime.h>
+#include <stddef.h>
+#include <stdint.h>
+
+#include <string>
+#include <vector>
+
+namespace bz {
+
+// ---- shape of one commit (flock-core/src/pcs/commit.rs:53-92) -------------
+struct Shape {
+    int log_msg_len = 0;    // m - 7
+    int log_inv_rate = 0;   // r
+    int log_lanes = 0;      // log_batch_size (a)
+    int hash_kind = 1;      // 0 sha256, 1 blake3
+    int log_dim() const { return log_msg_len - log_lanes; }        // b
+    int k_code() const { return log_dim() + log_inv_rate; }        // ell
+    size_t msg_words() const { return (size_t)1 << log_msg_len; }
+    size_t cw_words() const { return (size_t)1 << (log_msg_len + log_inv_rate); }
+    size_t n_leaves() const { return (size_t)1 << k_code(); }
+    size_t leaf_bytes() const { return (size_t)16 << log_lanes; }
+    size_t tree_nodes() const { return 2 * n_leaves() - 1; }
+};
+
+// Optional per-launch event marks (phase timing for the benchmark).
+struct LaunchLog {
+    cudaStream_t st = nullptr;
+    std::vector<std::string> names;
+    std::vector<cudaEvent_t> events;
+    void mark(const char *name) {
+        cudaEvent_t e;
+        cudaEventCreate(&e);
+        cudaEventRecord(e, st);
+        names.emplace_back(name);
+        events.push_back(e);
+    }
+    ~LaunchLog() {
+        for (auto e : events) cudaEventDestroy(e);
+    }
+};
+
+// ---- NTT schedule ----------------------------------------------------------
+// Packed as: bits 0..3 = number of deep (shift-and-XOR) layers D (0..4),
+// bit 4 = use radix-2 passes only for the table layers, bit 5 = force the
+// generic one-layer-per-launch kernels (reference / fallback path).
+enum : uint32_t { SCHED_DEEP_MASK = 0xF, SCHED_RADIX2 = 0x10, SCHED_GENERIC = 0x20 };
+uint32_t default_schedule(const Shape &s);
+
+// Twiddle heap for AdditiveNttF128::standard(ell): tw[(1 << l) + b] =
+// twiddle(l, b) for 0 <= l < ell, 0 <= b < 2^l (entry 0 unused).
+std::vector<uint64_t> twiddle_heap(int ell);
+
+// Enqueue the forward interleaved NTT from layer r with the replicate fill
+// fused (reads d_msg, writes d_cw).  Returns the number of kernels launched.
+int launch_ntt(const Shape &s, uint32_t schedule, const uint4 *d_msg, uint4 *d_cw,
+               const uint4 *d_tw, cudaStream_t st, int num_sms, LaunchLog *log = nullptr);
+
+// Merkle tree over the codeword rows (leaves = positions).  d_scratch must hold
+// merkle_scratch_bytes(s).  Returns kernels launched.
+size_t merkle_scratch_bytes(const Shape &s);
+int launch_merkle(const Shape &s, const uint4 *d_cw, uint8_t *d_tree, uint8_t *d_scratch,
+                  cudaStream_t st, int num_sms, LaunchLog *log = nullptr);
+
+// Gathers: rows of the codeword and arbitrary tree nodes.
+int launch_gather_rows(const uint4 *d_cw, int log_lanes, const uint64_t *d_pos, size_t q,
+                       uint4 *d_out, cudaStream_t st);
+int launch_gather_nodes(const uint8_t *d_tree, const uint64_t *d_idx, size_t n, uint8_t *d_out,
+                        cudaStream_t st);
+
+// Folds.  d_partials holds fold_partials_bytes(n) bytes.
+size_t fold_partials_bytes(size_t n);
+int launch_fold_and_msg(const uint4 *d_f, const uint4 *d_b, size_t n, uint4 r, uint4 *d_nf,
+                        uint4 *d_nb, uint64_t *d_partials, uint64_t *d_msg_out, cudaStream_t st,
+                        int num_sms);
+int launch_round_msg(const uint4 *d_f, const uint4 *d_b, size_t n, uint64_t *d_partials,
+                     uint64_t *d_msg_out, cudaStream_t st, int num_sms);
+int launch_partial_eval_round(const uint4 *d_in, size_t n, uint4 r, uint4 *d_out,
+                              cudaStream_t st);
+int launch_build_eq(const uint4 *d_point_dev, size_t k, uint4 *d_out, cudaStream_t st);
+int launch_sv_fold(const uint4 *d_packed, const uint4 *d_eq, size_t n, uint64_t *d_partials,
+                   uint4 *d_sv, cudaStream_t st, int num_sms);
+size_t sv_partials_bytes(size_t n, int num_sms);
+int launch_phi(const uint4 *d_eq_hi, size_t n, const uint4 *d_eq_r2, uint4 *d_out,
+               cudaStream_t st);
+
+int launch_chacha(uint64_t seed, uint64_t first_word, uint4 *d_out, size_t n_words,
+                  cudaStream_t st);
+
+// One-time kernel attributes (large dynamic shared memory), called when a
+// context is created so no attribute call happens during graph capture.
+void init_ntt_kernels();
+void init_fold_kernels();
+
+// Host GF(2^128) (twiddle tables, host-side checks of transcript values).
+void hgf_mul(const uint64_t a[2], const uint64_t b[2], uint64_t out[2]);
+void hgf_inv(const uint64_t a[2], uint64_t out[2]);
+
+}  // namespace bz

@@ -1,0 +1,329 @@
+// Opening-time kernels: sumcheck lane folds and messages
+// (flock-core/src/pcs/ligerito.rs), the ring-switch passes (BitZ
+// src/ligerito.rs), the eq table (src/poly/utils.rs) and the ChaCha20 input
+// generator.
+//
+// Field sums are exact and order independent, so partial sums per CTA are
+// XOR-reduced as unreduced 256-bit values and reduced once at the end, which
+// is bit-identical to the reference's per-term sums (ligerito.rs:2646-2649).
+#include <cuda_runtime.h>
+
+#include <algorithm>
+
+#include "bz_internal.h"
+#include "gf128.cuh"
+
+namespace bz {
+
+__device__ __forceinline__ void warp_xor_wide(gf_wide &a) {
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+#pragma unroll
+        for (int i = 0; i < 4; ++i) a.w[i] ^= __shfl_xor_sync(0xffffffffu, a.w[i], o);
+    }
+}
+
+// Reduce two wide accumulators over the CTA and store 8 words at out.
+__device__ void cta_store_pair(gf_wide u0, gf_wide u2, uint64_t *out) {
+    __shared__ uint64_t red[32][8];
+    warp_xor_wide(u0);
+    warp_xor_wide(u2);
+    const int w = threadIdx.x >> 5, ln = threadIdx.x & 31;
+    if (ln == 0) {
+#pragma unroll
+        for (int i = 0; i < 4; ++i) {
+            red[w][i] = u0.w[i];
+            red[w][4 + i] = u2.w[i];
+        }
+    }
+    __syncthreads();
+    if (threadIdx.x < 8) {
+        uint64_t acc = 0;
+        const int nw = blockDim.x >> 5;
+        for (int k = 0; k < nw; ++k) acc ^= red[k][threadIdx.x];
+        out[threadIdx.x] = acc;
+    }
+}
+
+// nf[j] = f[2j] + (f[2j] + f[2j+1]) * r (same for b); thread k produces the
+// folded pair (2k, 2k+1) and its message terms.
+__global__ void __launch_bounds__(256) fold_and_msg_kernel(const uint4 *f, const uint4 *b,
+                                                           uint64_t half, uint4 r, uint4 *nf,
+                                                           uint4 *nb, uint64_t *partials) {
+    gf_wide u0 = gf_wide_zero(), u2 = gf_wide_zero();
+    const uint64_t pairs = half >> 1;
+    for (uint64_t k = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; k < pairs;
+         k += (uint64_t)gridDim.x * blockDim.x) {
+        const uint4 *fp = f + 4 * k, *bp = b + 4 * k;
+        const uint4 f0 = fp[0], f1 = fp[1], f2 = fp[2], f3 = fp[3];
+        const uint4 b0 = bp[0], b1 = bp[1], b2 = bp[2], b3 = bp[3];
+        const uint4 x0 = gf_add(f0, gf_mul(gf_add(f0, f1), r));
+        const uint4 x1 = gf_add(f2, gf_mul(gf_add(f2, f3), r));
+        const uint4 y0 = gf_add(b0, gf_mul(gf_add(b0, b1), r));
+        const uint4 y1 = gf_add(b2, gf_mul(gf_add(b2, b3), r));
+        nf[2 * k] = x0;
+        nf[2 * k + 1] = x1;
+        nb[2 * k] = y0;
+        nb[2 * k + 1] = y1;
+        gf_wide_xor(u0, gf_mul_wide(x0, y0));
+        gf_wide_xor(u2, gf_mul_wide(gf_add(x0, x1), gf_add(y0, y1)));
+    }
+    if (half == 1 && blockIdx.x == 0 && threadIdx.x == 0) {
+        nf[0] = gf_add(f[0], gf_mul(gf_add(f[0], f[1]), r));
+        nb[0] = gf_add(b[0], gf_mul(gf_add(b[0], b[1]), r));
+    }
+    cta_store_pair(u0, u2, partials + (uint64_t)blockIdx.x * 8);
+}
+
+__global__ void __launch_bounds__(256) round_msg_kernel(const uint4 *f, const uint4 *b,
+                                                        uint64_t pairs, uint64_t *partials) {
+    gf_wide u0 = gf_wide_zero(), u2 = gf_wide_zero();
+    for (uint64_t j = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; j < pairs;
+         j += (uint64_t)gridDim.x * blockDim.x) {
+        const uint4 f0 = f[2 * j], f1 = f[2 * j + 1], b0 = b[2 * j], b1 = b[2 * j + 1];
+        gf_wide_xor(u0, gf_mul_wide(f0, b0));
+        gf_wide_xor(u2, gf_mul_wide(gf_add(f0, f1), gf_add(b0, b1)));
+    }
+    cta_store_pair(u0, u2, partials + (uint64_t)blockIdx.x * 8);
+}
+
+// Final XOR of per-CTA partials and the single reduction: out = {u0, u2}.
+__global__ void finish_msg_kernel(const uint64_t *partials, int n, uint64_t *out) {
+    __shared__ uint64_t acc[8];
+    if (threadIdx.x < 8) {
+        uint64_t a = 0;
+        for (int i = 0; i < n; ++i) a ^= partials[(uint64_t)i * 8 + threadIdx.x];
+        acc[threadIdx.x] = a;
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        gf_wide w0, w2;
+        for (int i = 0; i < 4; ++i) {
+            w0.w[i] = acc[i];
+            w2.w[i] = acc[4 + i];
+        }
+        const uint4 u0 = gf_reduce(w0), u2 = gf_reduce(w2);
+        out[0] = lo64(u0);
+        out[1] = hi64(u0);
+        out[2] = lo64(u2);
+        out[3] = hi64(u2);
+    }
+}
+
+static int msg_grid(uint64_t work, int num_sms) {
+    const uint64_t g = (work + 255) / 256;
+    return (int)std::max<uint64_t>(1, std::min<uint64_t>(g, (uint64_t)num_sms * 4));
+}
+
+size_t fold_partials_bytes(size_t n) {
+    (void)n;
+    return (size_t)1024 * 8 * sizeof(uint64_t);  // up to 1024 CTAs
+}
+
+int launch_fold_and_msg(const uint4 *d_f, const uint4 *d_b, size_t n, uint4 r, uint4 *d_nf,
+                        uint4 *d_nb, uint64_t *d_partials, uint64_t *d_msg_out, cudaStream_t st,
+                        int num_sms) {
+    const uint64_t half = n / 2;
+    const int grid = std::min(msg_grid(half / 2, num_sms), 1024);
+    fold_and_msg_kernel<<<grid, 256, 0, st>>>(d_f, d_b, half, r, d_nf, d_nb, d_partials);
+    finish_msg_kernel<<<1, 32, 0, st>>>(d_partials, grid, d_msg_out);
+    return 2;
+}
+
+int launch_round_msg(const uint4 *d_f, const uint4 *d_b, size_t n, uint64_t *d_partials,
+                     uint64_t *d_msg_out, cudaStream_t st, int num_sms) {
+    const uint64_t pairs = n / 2;
+    const int grid = std::min(msg_grid(pairs, num_sms), 1024);
+    round_msg_kernel<<<grid, 256, 0, st>>>(d_f, d_b, pairs, d_partials);
+    finish_msg_kernel<<<1, 32, 0, st>>>(d_partials, grid, d_msg_out);
+    return 2;
+}
+
+// One partial_eval_lsb round: out[i] = in[2i] + (in[2i] + in[2i+1]) * r
+// (= in[2i]*(1+r) + in[2i+1]*r exactly, ligerito.rs:1686-1691).
+__global__ void partial_eval_round_kernel(const uint4 *in, uint64_t half, uint4 r, uint4 *out) {
+    for (uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; i < half;
+         i += (uint64_t)gridDim.x * blockDim.x) {
+        const uint4 v0 = in[2 * i], v1 = in[2 * i + 1];
+        out[i] = gf_add(v0, gf_mul(gf_add(v0, v1), r));
+    }
+}
+
+int launch_partial_eval_round(const uint4 *d_in, size_t n, uint4 r, uint4 *d_out,
+                              cudaStream_t st) {
+    const uint64_t half = n / 2;
+    const unsigned grid = (unsigned)std::min<uint64_t>((half + 255) / 256, 8192);
+    partial_eval_round_kernel<<<std::max(grid, 1u), 256, 0, st>>>(d_in, half, r, d_out);
+    return 1;
+}
+
+// eq table rounds: entries [0, half) double into [0, 2 half).
+__global__ void eq_round_kernel(uint4 *eq, uint64_t half, const uint4 *point, int i) {
+    const uint4 r = point[i];
+    for (uint64_t j = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; j < half;
+         j += (uint64_t)gridDim.x * blockDim.x) {
+        const uint4 p = eq[j];
+        const uint4 one = gf_mul(p, r);
+        eq[half + j] = one;
+        eq[j] = gf_add(p, one);
+    }
+}
+
+__global__ void eq_init_kernel(uint4 *eq) { eq[0] = make_uint4(1, 0, 0, 0); }
+
+int launch_build_eq(const uint4 *d_point, size_t k, uint4 *d_out, cudaStream_t st) {
+    eq_init_kernel<<<1, 1, 0, st>>>(d_out);
+    for (size_t i = 0; i < k; ++i) {
+        const uint64_t half = (uint64_t)1 << i;
+        const unsigned grid = (unsigned)std::min<uint64_t>((half + 255) / 256, 8192);
+        eq_round_kernel<<<std::max(grid, 1u), 256, 0, st>>>(d_out, half, d_point, (int)i);
+    }
+    return (int)k + 1;
+}
+
+// sv[j] = sum_y eq[y] * bit_j(P[y]) (src/ligerito.rs:317-375).  128 threads
+// per CTA, one per output bit j; the CTA stages a tile of (P, eq) in shared
+// memory and every thread scans it (broadcast reads).
+constexpr int kSvTile = 256;
+__global__ void __launch_bounds__(128) sv_fold_kernel(const uint4 *packed, const uint4 *eq,
+                                                      uint64_t n, uint4 *partials) {
+    __shared__ uint4 sp[kSvTile], se[kSvTile];
+    const int j = threadIdx.x;
+    const int wsel = j >> 5;
+    const uint32_t bit = j & 31;
+    uint4 acc = make_uint4(0, 0, 0, 0);
+    for (uint64_t base = (uint64_t)blockIdx.x * kSvTile; base < n;
+         base += (uint64_t)gridDim.x * kSvTile) {
+        __syncthreads();
+        for (int i = threadIdx.x; i < kSvTile; i += blockDim.x) {
+            const uint64_t y = base + i;
+            sp[i] = y < n ? packed[y] : make_uint4(0, 0, 0, 0);
+            se[i] = y < n ? eq[y] : make_uint4(0, 0, 0, 0);
+        }
+        __syncthreads();
+#pragma unroll 8
+        for (int i = 0; i < kSvTile; ++i) {
+            const uint4 p = sp[i];
+            const uint32_t w = wsel == 0 ? p.x : wsel == 1 ? p.y : wsel == 2 ? p.z : p.w;
+            const uint32_t m = 0u - ((w >> bit) & 1u);
+            const uint4 e = se[i];
+            acc.x ^= e.x & m;
+            acc.y ^= e.y & m;
+            acc.z ^= e.z & m;
+            acc.w ^= e.w & m;
+        }
+    }
+    partials[(uint64_t)blockIdx.x * 128 + j] = acc;
+}
+
+__global__ void sv_finish_kernel(const uint4 *partials, int n_ctas, uint4 *sv) {
+    const int j = threadIdx.x;
+    uint4 acc = make_uint4(0, 0, 0, 0);
+    for (int c = 0; c < n_ctas; ++c) acc = gf_add(acc, partials[(uint64_t)c * 128 + j]);
+    sv[j] = acc;
+}
+
+size_t sv_partials_bytes(size_t n, int num_sms) {
+    (void)n;
+    return (size_t)num_sms * 4 * 128 * 16;
+}
+
+int launch_sv_fold(const uint4 *d_packed, const uint4 *d_eq, size_t n, uint64_t *d_partials,
+                   uint4 *d_sv, cudaStream_t st, int num_sms) {
+    const uint64_t tiles = (n + kSvTile - 1) / kSvTile;
+    const int grid = (int)std::max<uint64_t>(1, std::min<uint64_t>(tiles, (uint64_t)num_sms * 4));
+    uint4 *parts = reinterpret_cast<uint4 *>(d_partials);
+    sv_fold_kernel<<<grid, 128, 0, st>>>(d_packed, d_eq, n, parts);
+    sv_finish_kernel<<<1, 128, 0, st>>>(parts, grid, d_sv);
+    return 2;
+}
+
+// phi_from_words with phi_byte_tables (src/ligerito.rs:384-427): 16 byte
+// tables T[pos][v] = sum_{bit q of v} eq_r2[8 pos + q] in shared memory.
+__global__ void __launch_bounds__(256) phi_kernel(const uint4 *eq_hi, uint64_t n,
+                                                  const uint4 *eq_r2, uint4 *out) {
+    extern __shared__ uint4 tbl[];  // 16 * 256
+    for (int u = threadIdx.x; u < 16 * 256; u += blockDim.x) {
+        const int pos = u >> 8, v = u & 255;
+        uint4 acc = make_uint4(0, 0, 0, 0);
+        for (int q = 0; q < 8; ++q)
+            if ((v >> q) & 1) acc = gf_add(acc, eq_r2[8 * pos + q]);
+        tbl[u] = acc;
+    }
+    __syncthreads();
+    for (uint64_t y = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; y < n;
+         y += (uint64_t)gridDim.x * blockDim.x) {
+        const uint4 w = eq_hi[y];
+        const uint32_t ws[4] = {w.x, w.y, w.z, w.w};
+        uint4 acc = make_uint4(0, 0, 0, 0);
+#pragma unroll
+        for (int pos = 0; pos < 16; ++pos) {
+            const uint32_t v = (ws[pos >> 2] >> (8 * (pos & 3))) & 0xff;
+            acc = gf_add(acc, tbl[pos * 256 + v]);
+        }
+        out[y] = acc;
+    }
+}
+
+void init_fold_kernels() {
+    cudaFuncSetAttribute(phi_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, 65536);
+}
+
+int launch_phi(const uint4 *d_eq_hi, size_t n, const uint4 *d_eq_r2, uint4 *d_out,
+               cudaStream_t st) {
+    const unsigned grid = (unsigned)std::max<uint64_t>(
+        1, std::min<uint64_t>((n + 255) / 256, 2048));
+    phi_kernel<<<grid, 256, 65536, st>>>(d_eq_hi, n, d_eq_r2, d_out);
+    return 1;
+}
+
+// ---------------------------------------------------------------------------
+// ChaCha20 (RFC 8439 section 2.3): one 64-byte block per thread = 4 words.
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ uint32_t rotl(uint32_t x, int n) { return __funnelshift_l(x, x, n); }
+#define BZ_QR(a, b, c, d)                                 \
+    do {                                                  \
+        x[a] += x[b]; x[d] = rotl(x[d] ^ x[a], 16);       \
+        x[c] += x[d]; x[b] = rotl(x[b] ^ x[c], 12);       \
+        x[a] += x[b]; x[d] = rotl(x[d] ^ x[a], 8);        \
+        x[c] += x[d]; x[b] = rotl(x[b] ^ x[c], 7);        \
+    } while (0)
+
+__global__ void chacha_kernel(uint32_t k0, uint32_t k1, uint64_t first_word, uint4 *out,
+                              uint64_t n_words) {
+    const uint64_t first_blk = first_word >> 2;
+    const uint64_t last_blk = (first_word + n_words - 1) >> 2;
+    for (uint64_t blk = first_blk + (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
+         blk <= last_blk; blk += (uint64_t)gridDim.x * blockDim.x) {
+        uint32_t st[16] = {0x61707865u, 0x3320646eu, 0x79622d32u, 0x6b206574u, k0, k1, 0, 0,
+                           0, 0, 0, 0, (uint32_t)blk, 0, 0, 0};
+        uint32_t x[16];
+#pragma unroll
+        for (int i = 0; i < 16; ++i) x[i] = st[i];
+#pragma unroll
+        for (int i = 0; i < 10; ++i) {
+            BZ_QR(0, 4, 8, 12); BZ_QR(1, 5, 9, 13); BZ_QR(2, 6, 10, 14); BZ_QR(3, 7, 11, 15);
+            BZ_QR(0, 5, 10, 15); BZ_QR(1, 6, 11, 12); BZ_QR(2, 7, 8, 13); BZ_QR(3, 4, 9, 14);
+        }
+#pragma unroll
+        for (int i = 0; i < 16; ++i) x[i] += st[i];
+#pragma unroll
+        for (int q = 0; q < 4; ++q) {
+            const uint64_t w = blk * 4 + q;
+            if (w >= first_word && w < first_word + n_words)
+                out[w - first_word] = make_uint4(x[4 * q], x[4 * q + 1], x[4 * q + 2], x[4 * q + 3]);
+        }
+    }
+}
+
+int launch_chacha(uint64_t seed, uint64_t first_word, uint4 *d_out, size_t n_words,
+                  cudaStream_t st) {
+    if (n_words == 0) return 0;
+    const uint64_t blocks = ((first_word + n_words - 1) >> 2) - (first_word >> 2) + 1;
+    const unsigned grid = (unsigned)std::min<uint64_t>((blocks + 255) / 256, 8192);
+    chacha_kernel<<<grid, 256, 0, st>>>((uint32_t)seed, (uint32_t)(seed >> 32), first_word, d_out,
+                                        n_words);
+    return 1;
+}
+
+}  // namespace bz

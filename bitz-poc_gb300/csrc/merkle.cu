@@ -1,0 +1,417 @@
+// Merkle tree over codeword rows (flock-core/src/merkle.rs:558-596,
+// commit.rs:283-297): leaf i = the 16 * 2^log_lanes bytes of position i,
+// flat layout [leaves .., level k-1 .., root].
+//
+// BLAKE3 leaves are non-root chaining values with BLAKE3's own chunk tree
+// (merkle.rs:160-201).  For a leaf of C = L/64 >= 1 full 1 KiB chunks (C a
+// power of two), the leaf CV is a perfect binary tree of PARENT merges over
+// the C chunk CVs (chunk counter = chunk index inside the leaf), and the
+// Merkle tree above the leaves is the same PARENT merge, so one CTA hashes
+// 256 chunks (one per thread) and folds them in shared memory straight into
+// leaf CVs.  Leaves shorter than 1 KiB are one partial chunk (counter 0).
+// SHA-256 leaves are sha256(row) (merkle.rs:213) and parents sha256(l || r).
+#include <cuda_runtime.h>
+
+#include <algorithm>
+
+#include "bz_internal.h"
+#include "hash.cuh"
+
+namespace bz {
+
+// ---------------------------------------------------------------------------
+// BLAKE3 leaves, C >= 1 chunks per leaf, C <= 256.
+// Each thread computes one chunk CV; the CTA (256 threads = 256 chunks =
+// 256 / C leaves) reduces groups of C CVs to leaf CVs in shared memory.
+// ---------------------------------------------------------------------------
+__global__ void __launch_bounds__(256) b3_leaves_chunked(const uint4 *cw, int log_lanes,
+                                                         uint64_t n_chunks, uint32_t *tree_leaves,
+                                                         int log_c) {
+    __shared__ uint32_t cvs[256][9];  // padded rows
+    const uint64_t chunk = (uint64_t)blockIdx.x * 256 + threadIdx.x;
+    const uint32_t c_in_leaf = (uint32_t)(chunk & ((1u << log_c) - 1));
+    uint32_t cv[8];
+#pragma unroll
+    for (int i = 0; i < 8; ++i) cv[i] = kIV[i];
+    if (chunk < n_chunks) {
+        const uint4 *p = cw + chunk * 64;  // 64 elements = 1024 bytes
+#pragma unroll 1
+        for (int blk = 0; blk < 16; ++blk) {
+            uint32_t m[16];
+#pragma unroll
+            for (int q = 0; q < 4; ++q) {
+                const uint4 v = __ldcs(p + blk * 4 + q);
+                m[4 * q] = v.x;
+                m[4 * q + 1] = v.y;
+                m[4 * q + 2] = v.z;
+                m[4 * q + 3] = v.w;
+            }
+            const uint32_t flags = (blk == 0 ? B3_CHUNK_START : 0) | (blk == 15 ? B3_CHUNK_END : 0);
+            b3_compress_cv(cv, m, c_in_leaf, 64, flags);
+        }
+    }
+#pragma unroll
+    for (int i = 0; i < 8; ++i) cvs[threadIdx.x][i] = cv[i];
+    __syncthreads();
+    // In-leaf reduction: level s merges nodes (2j, 2j+1) within groups of C.
+    for (int s = 0; s < log_c; ++s) {
+        const int stride = 1 << s;
+        const int t = threadIdx.x;
+        if ((t & ((stride << 1) - 1)) == 0 && t + stride < 256) {
+            uint32_t out[8];
+            b3_parent(cvs[t], cvs[t + stride], out);
+#pragma unroll
+            for (int i = 0; i < 8; ++i) cvs[t][i] = out[i];
+        }
+        __syncthreads();
+    }
+    if ((threadIdx.x & ((1 << log_c) - 1)) == 0 && chunk < n_chunks) {
+        const uint64_t leaf = chunk >> log_c;
+#pragma unroll
+        for (int i = 0; i < 8; ++i) tree_leaves[leaf * 8 + i] = cvs[threadIdx.x][i];
+    }
+}
+
+// BLAKE3 leaves of at most one chunk (leaf_bytes = 16 * 2^log_lanes <= 1024).
+__global__ void b3_leaves_small(const uint4 *cw, int log_lanes, uint64_t n_leaves,
+                                uint32_t *tree_leaves) {
+    const uint64_t leaf = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (leaf >= n_leaves) return;
+    const uint32_t elems = 1u << log_lanes;  // 16-byte elements
+    const uint32_t bytes = elems * 16;
+    const uint32_t nblk = (bytes + 63) / 64;
+    const uint4 *p = cw + leaf * elems;
+    uint32_t cv[8];
+#pragma unroll
+    for (int i = 0; i < 8; ++i) cv[i] = kIV[i];
+    for (uint32_t blk = 0; blk < nblk; ++blk) {
+        uint32_t m[16];
+#pragma unroll
+        for (int q = 0; q < 4; ++q) {
+            const uint32_t e = blk * 4 + q;
+            const uint4 v = e < elems ? p[e] : make_uint4(0, 0, 0, 0);
+            m[4 * q] = v.x;
+            m[4 * q + 1] = v.y;
+            m[4 * q + 2] = v.z;
+            m[4 * q + 3] = v.w;
+        }
+        const uint32_t len = min(64u, bytes - blk * 64);
+        const uint32_t flags =
+            (blk == 0 ? B3_CHUNK_START : 0) | (blk == nblk - 1 ? B3_CHUNK_END : 0);
+        b3_compress_cv(cv, m, 0, len, flags);
+    }
+#pragma unroll
+    for (int i = 0; i < 8; ++i) tree_leaves[leaf * 8 + i] = cv[i];
+}
+
+// Generic BLAKE3 chunk CVs into scratch (leaves longer than 256 chunks).
+__global__ void b3_chunk_cvs(const uint4 *cw, uint64_t n_chunks, int log_c, uint32_t *out) {
+    const uint64_t chunk = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (chunk >= n_chunks) return;
+    const uint32_t c_in_leaf = (uint32_t)(chunk & ((1ull << log_c) - 1));
+    uint32_t cv[8];
+#pragma unroll
+    for (int i = 0; i < 8; ++i) cv[i] = kIV[i];
+    const uint4 *p = cw + chunk * 64;
+#pragma unroll 1
+    for (int blk = 0; blk < 16; ++blk) {
+        uint32_t m[16];
+#pragma unroll
+        for (int q = 0; q < 4; ++q) {
+            const uint4 v = __ldcs(p + blk * 4 + q);
+            m[4 * q] = v.x;
+            m[4 * q + 1] = v.y;
+            m[4 * q + 2] = v.z;
+            m[4 * q + 3] = v.w;
+        }
+        const uint32_t flags = (blk == 0 ? B3_CHUNK_START : 0) | (blk == 15 ? B3_CHUNK_END : 0);
+        b3_compress_cv(cv, m, c_in_leaf, 64, flags);
+    }
+#pragma unroll
+    for (int i = 0; i < 8; ++i) out[chunk * 8 + i] = cv[i];
+}
+
+// ---------------------------------------------------------------------------
+// Parent levels.  One CTA takes 2^k consecutive nodes of level `in` and
+// writes every node of the k levels above them (each level into its own slot
+// of the flat tree), so a 2^20-leaf tree needs 3 launches instead of 20.
+// kind: 0 = SHA-256, 1 = BLAKE3.
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ void sha256_pair(const uint32_t l[8], const uint32_t r[8],
+                                            uint32_t out[8]) {
+    uint32_t st[8] = {0x6a09e667, 0xbb67ae85, 0x3c6ef372, 0xa54ff53a,
+                      0x510e527f, 0x9b05688c, 0x1f83d9ab, 0x5be0cd19};
+    uint32_t w[16];
+#pragma unroll
+    for (int i = 0; i < 8; ++i) {
+        w[i] = bswap32(l[i]);
+        w[8 + i] = bswap32(r[i]);
+    }
+    sha256_compress(st, w);
+#pragma unroll
+    for (int i = 0; i < 16; ++i) w[i] = 0;
+    w[0] = 0x80000000u;
+    w[15] = 512;
+    sha256_compress(st, w);
+#pragma unroll
+    for (int i = 0; i < 8; ++i) out[i] = bswap32(st[i]);
+}
+
+__device__ __forceinline__ void hash_pair(int kind, const uint32_t l[8], const uint32_t r[8],
+                                          uint32_t out[8]) {
+    if (kind == 1) b3_parent(l, r, out);
+    else sha256_pair(l, r, out);
+}
+
+// in: n_in nodes (32 B each); outputs levels written at out_levels[0..k-1]
+// with level j holding n_in >> (j+1) nodes.  blockDim = 256, each CTA covers
+// 512 input nodes (or fewer at the top).
+struct LevelsArgs {
+    const uint32_t *in;
+    uint32_t *out[10];
+    uint64_t n_in;
+    int k;  // levels to produce (<= 9)
+    int kind;
+};
+
+__global__ void __launch_bounds__(256) merkle_levels(LevelsArgs a) {
+    __shared__ uint32_t nodes[256][9];
+    const uint64_t base_in = (uint64_t)blockIdx.x * 512;
+    const int t = threadIdx.x;
+    // level 0 of this CTA: parents of input pairs
+    uint64_t n_lvl = a.n_in >> 1;  // nodes at the first output level
+    {
+        const uint64_t j = ((uint64_t)blockIdx.x * 256) + t;
+        uint32_t o[8];
+        if (j < n_lvl) {
+            uint32_t l[8], r[8];
+            const uint4 *pl = reinterpret_cast<const uint4 *>(a.in + (base_in + 2 * t) * 8);
+            const uint4 l0 = pl[0], l1 = pl[1], r0 = pl[2], r1 = pl[3];
+            l[0] = l0.x; l[1] = l0.y; l[2] = l0.z; l[3] = l0.w;
+            l[4] = l1.x; l[5] = l1.y; l[6] = l1.z; l[7] = l1.w;
+            r[0] = r0.x; r[1] = r0.y; r[2] = r0.z; r[3] = r0.w;
+            r[4] = r1.x; r[5] = r1.y; r[6] = r1.z; r[7] = r1.w;
+            hash_pair(a.kind, l, r, o);
+            uint4 *po = reinterpret_cast<uint4 *>(a.out[0] + j * 8);
+            po[0] = make_uint4(o[0], o[1], o[2], o[3]);
+            po[1] = make_uint4(o[4], o[5], o[6], o[7]);
+#pragma unroll
+            for (int i = 0; i < 8; ++i) nodes[t][i] = o[i];
+        }
+    }
+    __syncthreads();
+    uint64_t cta_nodes = n_lvl < 256 ? n_lvl : 256;  // nodes of this CTA at the current level
+    for (int lv = 1; lv < a.k; ++lv) {
+        const uint64_t half = cta_nodes >> 1;
+        const bool active = (uint64_t)t < half;
+        uint32_t o[8];
+        if (active) {
+            hash_pair(a.kind, nodes[2 * t], nodes[2 * t + 1], o);
+            const uint64_t j = (uint64_t)blockIdx.x * (256 >> lv) + t;
+            uint4 *po = reinterpret_cast<uint4 *>(a.out[lv] + j * 8);
+            po[0] = make_uint4(o[0], o[1], o[2], o[3]);
+            po[1] = make_uint4(o[4], o[5], o[6], o[7]);
+        }
+        __syncthreads();  // every read of this level precedes the overwrite
+        if (active) {
+#pragma unroll
+            for (int i = 0; i < 8; ++i) nodes[t][i] = o[i];
+        }
+        __syncthreads();
+        cta_nodes = half;
+    }
+}
+
+// SHA-256 leaves: one thread per leaf, sequential over the row.
+__global__ void sha_leaves(const uint4 *cw, int log_lanes, uint64_t n_leaves,
+                           uint32_t *tree_leaves) {
+    const uint64_t leaf = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (leaf >= n_leaves) return;
+    const uint64_t elems = (uint64_t)1 << log_lanes;
+    const uint64_t bytes = elems * 16;
+    const uint4 *p = cw + leaf * elems;
+    uint32_t st[8] = {0x6a09e667, 0xbb67ae85, 0x3c6ef372, 0xa54ff53a,
+                      0x510e527f, 0x9b05688c, 0x1f83d9ab, 0x5be0cd19};
+    const uint64_t full = bytes / 64;  // full 64-byte blocks
+    for (uint64_t blk = 0; blk < full; ++blk) {
+        uint32_t w[16];
+#pragma unroll
+        for (int q = 0; q < 4; ++q) {
+            const uint4 v = p[blk * 4 + q];
+            w[4 * q] = bswap32(v.x);
+            w[4 * q + 1] = bswap32(v.y);
+            w[4 * q + 2] = bswap32(v.z);
+            w[4 * q + 3] = bswap32(v.w);
+        }
+        sha256_compress(st, w);
+    }
+    // tail: remaining (bytes % 64) bytes, then 0x80, zeros, 64-bit length
+    const uint32_t rem = (uint32_t)(bytes - full * 64);  // 0, 16, 32 or 48
+    uint32_t w[16];
+#pragma unroll
+    for (int i = 0; i < 16; ++i) w[i] = 0;
+    for (uint32_t e = 0; e < rem / 16; ++e) {
+        const uint4 v = p[full * 4 + e];
+        w[4 * e] = bswap32(v.x);
+        w[4 * e + 1] = bswap32(v.y);
+        w[4 * e + 2] = bswap32(v.z);
+        w[4 * e + 3] = bswap32(v.w);
+    }
+    w[rem / 4] = 0x80000000u;
+    const uint64_t bitlen = bytes * 8;
+    if (rem + 9 > 64) {
+        sha256_compress(st, w);
+#pragma unroll
+        for (int i = 0; i < 16; ++i) w[i] = 0;
+    }
+    w[14] = (uint32_t)(bitlen >> 32);
+    w[15] = (uint32_t)bitlen;
+    sha256_compress(st, w);
+#pragma unroll
+    for (int i = 0; i < 8; ++i) tree_leaves[leaf * 8 + i] = bswap32(st[i]);
+}
+
+size_t merkle_scratch_bytes(const Shape &s) {
+    if (s.hash_kind == 1 && s.log_lanes > 14) {
+        const size_t chunks = s.cw_words() / 64;
+        return chunks * 32 * 2;
+    }
+    return 0;
+}
+
+// Build all parent levels above `n_leaves` leaves stored at tree[0..).
+static int launch_levels(uint32_t *tree, uint64_t n_leaves, int kind, cudaStream_t st,
+                         LaunchLog *log) {
+    int launches = 0;
+    uint64_t in_off = 0, n_in = n_leaves;
+    while (n_in > 1) {
+        int k = 0;
+        uint64_t n = n_in;
+        while (n > 1 && k < 9) {
+            n >>= 1;
+            ++k;
+        }
+        LevelsArgs a;
+        a.in = tree + in_off * 8;
+        a.n_in = n_in;
+        a.k = k;
+        a.kind = kind;
+        uint64_t off = in_off + n_in, cnt = n_in >> 1;
+        for (int j = 0; j < k; ++j) {
+            a.out[j] = tree + off * 8;
+            off += cnt;
+            cnt >>= 1;
+        }
+        const uint64_t ctas = (n_in + 511) / 512;
+        merkle_levels<<<(unsigned)ctas, 256, 0, st>>>(a);
+        if (log) log->mark("merkle_levels");
+        ++launches;
+        // advance: the last produced level becomes the next input
+        uint64_t o = in_off + n_in, c = n_in >> 1;
+        for (int j = 0; j < k - 1; ++j) {
+            o += c;
+            c >>= 1;
+        }
+        in_off = o;
+        n_in = c;
+    }
+    return launches;
+}
+
+int launch_merkle(const Shape &s, const uint4 *d_cw, uint8_t *d_tree, uint8_t *d_scratch,
+                  cudaStream_t st, int num_sms, LaunchLog *log) {
+    auto mark = [&](const char *n) {
+        if (log) log->mark(n);
+    };
+    (void)num_sms;
+    const uint64_t n_leaves = s.n_leaves();
+    uint32_t *tree = reinterpret_cast<uint32_t *>(d_tree);
+    int launches = 0;
+    if (s.hash_kind == 1) {
+        if (s.log_lanes < 6) {
+            b3_leaves_small<<<(unsigned)((n_leaves + 255) / 256), 256, 0, st>>>(d_cw, s.log_lanes,
+                                                                             n_leaves, tree);
+            mark("b3_leaves_small");
+            ++launches;
+        } else if (s.log_lanes <= 14) {
+            const int log_c = s.log_lanes - 6;
+            const uint64_t n_chunks = n_leaves << log_c;
+            b3_leaves_chunked<<<(unsigned)((n_chunks + 255) / 256), 256, 0, st>>>(
+                d_cw, s.log_lanes, n_chunks, tree, log_c);
+            mark("b3_leaves_chunked");
+            ++launches;
+        } else {
+            const int log_c = s.log_lanes - 6;
+            const uint64_t n_chunks = n_leaves << log_c;
+            uint32_t *cvs = reinterpret_cast<uint32_t *>(d_scratch);
+            b3_chunk_cvs<<<(unsigned)((n_chunks + 255) / 256), 256, 0, st>>>(d_cw, n_chunks,
+                                                                           log_c, cvs);
+            mark("b3_chunk_cvs");
+            ++launches;
+            // reduce chunk CVs to leaf CVs: levels inside the scratch area,
+            // the last one written straight into the tree leaves.
+            uint32_t *bufs[2] = {cvs, cvs + n_chunks * 8};
+            uint64_t n = n_chunks;
+            int cur = 0;
+            for (int lv = 0; lv < log_c; ++lv) {
+                LevelsArgs a;
+                a.in = bufs[cur];
+                a.n_in = n;
+                a.k = 1;
+                a.kind = 1;
+                a.out[0] = (lv == log_c - 1) ? tree : bufs[cur ^ 1];
+                merkle_levels<<<(unsigned)((n + 511) / 512), 256, 0, st>>>(a);
+                mark("merkle_levels");
+                ++launches;
+                n >>= 1;
+                cur ^= 1;
+            }
+        }
+    } else {
+        sha_leaves<<<(unsigned)((n_leaves + 127) / 128), 128, 0, st>>>(d_cw, s.log_lanes,
+                                                                       n_leaves, tree);
+        mark("sha_leaves");
+        ++launches;
+    }
+    launches += launch_levels(tree, n_leaves, s.hash_kind, st, log);
+    return launches;
+}
+
+// ---------------------------------------------------------------------------
+// Gathers for openings.
+// ---------------------------------------------------------------------------
+__global__ void gather_rows(const uint4 *cw, int log_lanes, const uint64_t *pos, size_t q,
+                            uint4 *out) {
+    const uint64_t L = (uint64_t)1 << log_lanes;
+    const uint64_t total = q * L;
+    for (uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; i < total;
+         i += (uint64_t)gridDim.x * blockDim.x) {
+        const uint64_t r = i >> log_lanes, ln = i & (L - 1);
+        out[i] = cw[(pos[r] << log_lanes) | ln];
+    }
+}
+
+__global__ void gather_nodes(const uint4 *tree, const uint64_t *idx, size_t n, uint4 *out) {
+    const uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= 2 * n) return;
+    out[i] = tree[idx[i >> 1] * 2 + (i & 1)];
+}
+
+int launch_gather_rows(const uint4 *d_cw, int log_lanes, const uint64_t *d_pos, size_t q,
+                       uint4 *d_out, cudaStream_t st) {
+    if (q == 0) return 0;
+    const uint64_t total = (uint64_t)q << log_lanes;
+    const unsigned grid = (unsigned)std::min<uint64_t>((total + 255) / 256, 4096);
+    gather_rows<<<grid, 256, 0, st>>>(d_cw, log_lanes, d_pos, q, d_out);
+    return 1;
+}
+
+int launch_gather_nodes(const uint8_t *d_tree, const uint64_t *d_idx, size_t n, uint8_t *d_out,
+                        cudaStream_t st) {
+    if (n == 0) return 0;
+    gather_nodes<<<(unsigned)((2 * n + 255) / 256), 256, 0, st>>>(
+        reinterpret_cast<const uint4 *>(d_tree), d_idx, n, reinterpret_cast<uint4 *>(d_out));
+    return 1;
+}
+
+}  // namespace bz

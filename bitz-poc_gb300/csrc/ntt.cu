@@ -1,0 +1,474 @@
+// Forward interleaved additive NTT over GF(2^128) (LCH novel basis) for the
+// Reed-Solomon row encoding of the commit.
+//
+// Semantics follow flock-core/src/ntt/additive_ntt_f128.rs:
+//   * twiddle(l, b) = span of the normalized subspace-polynomial row
+//     evals[ell-l-1][1..] selected by the bits of b (:63-156);
+//   * layer l: blocks of 2^(ell-l) positions, pairs (row, row + half), every
+//     lane: u <- u + t*v ; v <- v + u (:243-274);
+//   * the first r layers of [msg, 0, ..] are copies, so the transform starts
+//     at layer r from 2^r replicas of the message (commit.rs:223-258).
+// Data layout: cw[pos * L + lane], 16 bytes per element, L = 2^log_lanes.
+//
+// GB300 mapping (integer pipes; no tensor cores -- nothing here is a dense
+// floating-point contraction):
+//   * "table" passes fuse two layers (radix-4) or one (radix-2) over the
+//     wide-twiddle layers.  Every thread owns one (block, row, lane) quad, so
+//     global loads/stores are 16-byte vectors coalesced across lanes.  A
+//     multiply by the block twiddle t is 16 lookups into a 64 KB shared-memory
+//     table T_k[x] = x * X^(8k) * t (one per byte k of the operand).  Tables
+//     are laid out so byte position k lives in bank group k mod 8 and each
+//     thread walks the byte positions in an order rotated by (lane mod 8):
+//     the 8 threads of a quarter-warp always hit 8 different bank groups, so
+//     the 128-bit lookups are bank-conflict free.  The first table pass reads
+//     the message and writes all 2^r replicas (the replicate fill is fused).
+//   * the "deep" pass runs the last D layers (D <= 4) on 2^D consecutive
+//     positions held in registers.  Their twiddles are narrow (at depth i the
+//     twiddle has at most ~2^i * ell bits: x^(j+1) at the deepest layer), so
+//     the multiply is a shift-and-XOR over the twiddle's set bits, with the
+//     twiddle warp-uniform.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cstring>
+
+#include "bz_internal.h"
+#include "gf128.cuh"
+
+namespace bz {
+
+// ===========================================================================
+// Host: normalized subspace-polynomial rows and the twiddle heap.
+// ===========================================================================
+std::vector<uint64_t> twiddle_heap(int ell) {
+    // evals[i][k], i < ell, k < ell - i (additive_ntt_f128.rs:66-100) for the
+    // basis {1, x, .., x^(ell-1)} (:136-140).
+    std::vector<uint64_t> ev(2 * (size_t)ell * ell, 0);
+    auto at = [&](int i, int k) { return &ev[2 * ((size_t)i * ell + k)]; };
+    for (int k = 0; k < ell; ++k) {
+        at(0, k)[0] = k < 64 ? (1ull << k) : 0;
+        at(0, k)[1] = k >= 64 ? (1ull << (k - 64)) : 0;
+    }
+    for (int i = 1; i < ell; ++i) {
+        for (int k = 1; k < ell - (i - 1); ++k) {
+            const uint64_t *p = at(i - 1, k), *p0 = at(i - 1, 0);
+            uint64_t s[2] = {p[0] ^ p0[0], p[1] ^ p0[1]};
+            hgf_mul(p, s, at(i, k - 1));
+        }
+    }
+    for (int i = 0; i < ell; ++i) {
+        uint64_t inv[2];
+        hgf_inv(at(i, 0), inv);
+        for (int k = 0; k < ell - i; ++k) {
+            uint64_t t[2];
+            hgf_mul(at(i, k), inv, t);
+            at(i, k)[0] = t[0];
+            at(i, k)[1] = t[1];
+        }
+    }
+    std::vector<uint64_t> heap(2 * ((size_t)1 << ell) + 2, 0);
+    for (int l = 0; l < ell; ++l) {
+        const size_t base = (size_t)1 << l;
+        const int row = ell - l - 1;
+        heap[2 * base] = 0;
+        heap[2 * base + 1] = 0;
+        for (size_t b = 1; b < base; ++b) {
+            const int j = __builtin_ctzll(b);
+            const uint64_t *prev = &heap[2 * (base + (b & (b - 1)))];
+            const uint64_t *e = at(row, 1 + j);
+            heap[2 * (base + b)] = prev[0] ^ e[0];
+            heap[2 * (base + b) + 1] = prev[1] ^ e[1];
+        }
+    }
+    return heap;
+}
+
+uint32_t default_schedule(const Shape &s) {
+    const int layers = s.log_dim();
+    const int deep = std::min(layers, 3);
+    return (uint32_t)deep;
+}
+
+// ===========================================================================
+// Device: 64 KB byte tables.
+// ===========================================================================
+constexpr int kT16Entries = 4096;  // 16 byte positions x 256 values
+
+// Byte offset of entry (k, x) inside one table.
+__device__ __forceinline__ uint32_t t16_off(uint32_t k, uint32_t x) {
+    return ((k >> 3) << 15) + (x << 7) + ((k & 7) << 4);
+}
+
+// Build the tables of n_tw twiddles (ts[i]) into tbl[i * 4096 ..].  `bases`
+// is 128 * n_tw uint4 of scratch.  Called by all threads; syncs inside.
+__device__ void t16_build(uint4 *tbl, uint4 *bases, const uint4 *ts, int n_tw) {
+    const int tid = threadIdx.x, nthr = blockDim.x;
+    for (int j = tid; j < 128 * n_tw; j += nthr) {
+        const int i = j >> 7, e = j & 127;
+        uint4 xe = make_uint4(0, 0, 0, 0);
+        const uint32_t bit = 1u << (e & 31);
+        if (e < 32) xe.x = bit;
+        else if (e < 64) xe.y = bit;
+        else if (e < 96) xe.z = bit;
+        else xe.w = bit;
+        bases[j] = gf_mul(ts[i], xe);  // t * X^e
+    }
+    __syncthreads();
+    for (int u = tid; u < 256 * n_tw; u += nthr) {
+        const int i = u >> 8, k = (u >> 4) & 15, hi = u & 15;
+        const uint4 *b = bases + i * 128 + 8 * k;
+        uint4 H = make_uint4(0, 0, 0, 0);
+#pragma unroll
+        for (int q = 0; q < 4; ++q)
+            if ((hi >> q) & 1) H = gf_add(H, b[4 + q]);
+        uint4 L[16];
+        L[0] = make_uint4(0, 0, 0, 0);
+        const uint4 b0 = b[0], b1 = b[1], b2 = b[2], b3 = b[3];
+#pragma unroll
+        for (int x = 1; x < 16; ++x) {
+            const int low = x & -x;
+            const uint4 bb = low == 1 ? b0 : low == 2 ? b1 : low == 4 ? b2 : b3;
+            L[x] = gf_add(L[x & (x - 1)], bb);
+        }
+        char *tb = reinterpret_cast<char *>(tbl + (size_t)i * kT16Entries);
+#pragma unroll
+        for (int lo = 0; lo < 16; ++lo)
+            *reinterpret_cast<uint4 *>(tb + t16_off(k, (hi << 4) | lo)) = gf_add(H, L[lo]);
+    }
+    __syncthreads();
+}
+
+// Per-thread lookup offsets: step m reads byte position (m + s) mod 16.
+struct T16Lane {
+    uint32_t off[16];
+    uint32_t s;
+    __device__ __forceinline__ void init() {
+        s = threadIdx.x & 7;
+#pragma unroll
+        for (int m = 0; m < 16; ++m) {
+            const uint32_t k = (m + s) & 15;
+            off[m] = ((k >> 3) << 15) + ((k & 7) << 4);
+        }
+    }
+    // v rotated right by 8*s bits: byte m of the result is byte (m+s)&15 of v.
+    __device__ __forceinline__ uint4 rot(uint4 v) const {
+        uint4 r = (s & 4) ? make_uint4(v.y, v.z, v.w, v.x) : v;
+        const uint32_t sh = (s & 3) << 3;
+        return make_uint4(__funnelshift_r(r.x, r.y, sh), __funnelshift_r(r.y, r.z, sh),
+                          __funnelshift_r(r.z, r.w, sh), __funnelshift_r(r.w, r.x, sh));
+    }
+    __device__ __forceinline__ uint4 mul(const char *tb, uint4 v) const {
+        const uint4 vr = rot(v);
+        uint4 acc = make_uint4(0, 0, 0, 0);
+#pragma unroll
+        for (int m = 0; m < 16; ++m) {
+            const uint32_t w = (m < 4) ? vr.x : (m < 8) ? vr.y : (m < 12) ? vr.z : vr.w;
+            const uint32_t x = __byte_perm(w, 0u, 0x4440u | (uint32_t)(m & 3));
+            const uint4 e = *reinterpret_cast<const uint4 *>(tb + (x << 7) + off[m]);
+            acc = gf_add(acc, e);
+        }
+        return acc;
+    }
+};
+
+struct TablePassArgs {
+    const uint4 *src;   // message (first pass) or codeword
+    uint4 *dst;         // codeword
+    const uint4 *tw;    // twiddle heap
+    int ell;            // k_code
+    int layer;          // first layer of this pass
+    int log_lanes;
+    int src_pos_bits;   // positions are masked to this many bits when reading src
+    uint64_t n_tasks;
+};
+
+// LAYERS = 2: radix-4 quad (a, b, c, d) at positions B*4Q + g*Q + rr:
+//   layer l   : (a,c), (b,d) with t_o = twiddle(l, B)
+//   layer l+1 : (a,b) with t_a = twiddle(l+1, 2B), (c,d) with t_b = twiddle(l+1, 2B+1)
+// (the fused 2-layer row op of additive_ntt_f128.rs:829-857, equal to the two
+// single layers applied in order).
+// LAYERS = 1: pair (p, p+H) at layer l with t = twiddle(l, B).
+template <int LAYERS>
+__global__ void __launch_bounds__(512, 1) ntt_table_pass(TablePassArgs a) {
+    extern __shared__ uint4 smem[];
+    constexpr int NT = LAYERS == 2 ? 3 : 1;
+    uint4 *tbl = smem;
+    uint4 *bases = smem + NT * kT16Entries;
+    __shared__ uint4 ts[3];
+    __shared__ int tz[3];
+
+    T16Lane lane_ctx;
+    lane_ctx.init();
+
+    const int log_q = a.ell - a.layer - LAYERS;  // log2 of the pair/quad stride
+    const int log_task_per_b = log_q + a.log_lanes;
+    const uint64_t lanes_mask = ((uint64_t)1 << a.log_lanes) - 1;
+    const uint64_t q_mask = ((uint64_t)1 << log_q) - 1;
+    const uint64_t src_mask = ((uint64_t)1 << a.src_pos_bits) - 1;
+
+    // Contiguous task range per CTA, aligned to blockDim.
+    const uint64_t chunks = a.n_tasks / blockDim.x;
+    const uint64_t c_beg = chunks * blockIdx.x / gridDim.x;
+    const uint64_t c_end = chunks * (blockIdx.x + 1) / gridDim.x;
+    int64_t cur_b = -1;
+
+    for (uint64_t c = c_beg; c < c_end; ++c) {
+        const uint64_t task = c * blockDim.x + threadIdx.x;
+        const uint64_t B = task >> log_task_per_b;  // uniform across the CTA
+        if ((int64_t)B != cur_b) {
+            __syncthreads();
+            if (threadIdx.x == 0) {
+                if (LAYERS == 2) {
+                    ts[0] = a.tw[((uint64_t)1 << a.layer) + B];
+                    ts[1] = a.tw[((uint64_t)1 << (a.layer + 1)) + 2 * B];
+                    ts[2] = a.tw[((uint64_t)1 << (a.layer + 1)) + 2 * B + 1];
+                } else {
+                    ts[0] = a.tw[((uint64_t)1 << a.layer) + B];
+                }
+                for (int i = 0; i < NT; ++i) tz[i] = gf_is_zero(ts[i]);
+            }
+            __syncthreads();
+            t16_build(tbl, bases, ts, NT);
+            cur_b = (int64_t)B;
+        }
+        const uint64_t rr = (task >> a.log_lanes) & q_mask;
+        const uint64_t ln = task & lanes_mask;
+        const char *T0 = reinterpret_cast<const char *>(tbl);
+        if (LAYERS == 2) {
+            uint64_t p[4];
+#pragma unroll
+            for (int g = 0; g < 4; ++g)
+                p[g] = (B << (log_q + 2)) + ((uint64_t)g << log_q) + rr;
+            uint4 v[4];
+#pragma unroll
+            for (int g = 0; g < 4; ++g)
+                v[g] = __ldcs(a.src + (((p[g] & src_mask) << a.log_lanes) | ln));
+            const char *T1 = T0 + kT16Entries * 16, *T2 = T1 + kT16Entries * 16;
+            if (!tz[0]) {
+                v[0] = gf_add(v[0], lane_ctx.mul(T0, v[2]));
+                v[1] = gf_add(v[1], lane_ctx.mul(T0, v[3]));
+            }
+            v[2] = gf_add(v[2], v[0]);
+            v[3] = gf_add(v[3], v[1]);
+            if (!tz[1]) v[0] = gf_add(v[0], lane_ctx.mul(T1, v[1]));
+            v[1] = gf_add(v[1], v[0]);
+            if (!tz[2]) v[2] = gf_add(v[2], lane_ctx.mul(T2, v[3]));
+            v[3] = gf_add(v[3], v[2]);
+#pragma unroll
+            for (int g = 0; g < 4; ++g) __stcs(a.dst + ((p[g] << a.log_lanes) | ln), v[g]);
+        } else {
+            const uint64_t p0 = (B << (log_q + 1)) + rr, p1 = p0 + ((uint64_t)1 << log_q);
+            uint4 u = __ldcs(a.src + (((p0 & src_mask) << a.log_lanes) | ln));
+            uint4 w = __ldcs(a.src + (((p1 & src_mask) << a.log_lanes) | ln));
+            if (!tz[0]) u = gf_add(u, lane_ctx.mul(T0, w));
+            w = gf_add(w, u);
+            __stcs(a.dst + ((p0 << a.log_lanes) | ln), u);
+            __stcs(a.dst + ((p1 << a.log_lanes) | ln), w);
+        }
+    }
+}
+
+struct DeepArgs {
+    const uint4 *src;
+    uint4 *dst;
+    const uint4 *tw;
+    int ell;
+    int log_lanes;
+    int src_pos_bits;
+    uint64_t n_tasks;  // 2^(ell - D) * L
+};
+
+// Last D layers on 2^D consecutive positions per thread (one lane).
+template <int D>
+__global__ void __launch_bounds__(256) ntt_deep_pass(DeepArgs a) {
+    constexpr int P = 1 << D;
+    const uint64_t lanes_mask = ((uint64_t)1 << a.log_lanes) - 1;
+    const uint64_t src_mask = ((uint64_t)1 << a.src_pos_bits) - 1;
+    for (uint64_t task = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; task < a.n_tasks;
+         task += (uint64_t)gridDim.x * blockDim.x) {
+        const uint64_t G = task >> a.log_lanes;
+        const uint64_t ln = task & lanes_mask;
+        uint4 v[P];
+#pragma unroll
+        for (int i = 0; i < P; ++i) {
+            const uint64_t pos = (G << D) + i;
+            v[i] = __ldcs(a.src + (((pos & src_mask) << a.log_lanes) | ln));
+        }
+#pragma unroll
+        for (int j = 0; j < D; ++j) {
+            const int l = a.ell - D + j;
+            constexpr int dummy = 0;
+            (void)dummy;
+            const int half = P >> (j + 1);
+#pragma unroll
+            for (int sb = 0; sb < (1 << j); ++sb) {
+                const uint64_t B = (G << j) | (uint64_t)sb;
+                const uint4 t = a.tw[((uint64_t)1 << l) + B];
+                const bool tz = gf_is_zero(t);
+#pragma unroll
+                for (int i = 0; i < half; ++i) {
+                    uint4 &u = v[sb * 2 * half + i];
+                    uint4 &w = v[sb * 2 * half + i + half];
+                    if (!tz) u = gf_add(u, gf_mul_narrow(w, t));
+                    w = gf_add(w, u);
+                }
+            }
+        }
+#pragma unroll
+        for (int i = 0; i < P; ++i) {
+            const uint64_t pos = (G << D) + i;
+            __stcs(a.dst + ((pos << a.log_lanes) | ln), v[i]);
+        }
+    }
+}
+
+// One layer, generic multiply: the reference path and the fallback for
+// shapes too small for the table passes.
+__global__ void ntt_generic_layer(const uint4 *src, uint4 *dst, const uint4 *tw, int ell,
+                                  int layer, int log_lanes, int src_pos_bits, uint64_t n_tasks) {
+    const int log_h = ell - layer - 1;
+    const uint64_t lanes_mask = ((uint64_t)1 << log_lanes) - 1;
+    const uint64_t src_mask = ((uint64_t)1 << src_pos_bits) - 1;
+    for (uint64_t task = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; task < n_tasks;
+         task += (uint64_t)gridDim.x * blockDim.x) {
+        const uint64_t ln = task & lanes_mask;
+        const uint64_t pair = task >> log_lanes;
+        const uint64_t B = pair >> log_h, rr = pair & (((uint64_t)1 << log_h) - 1);
+        const uint64_t p0 = (B << (log_h + 1)) + rr, p1 = p0 + ((uint64_t)1 << log_h);
+        const uint4 t = tw[((uint64_t)1 << layer) + B];
+        uint4 u = src[((p0 & src_mask) << log_lanes) | ln];
+        uint4 w = src[((p1 & src_mask) << log_lanes) | ln];
+        u = gf_add(u, gf_mul(w, t));
+        w = gf_add(w, u);
+        dst[(p0 << log_lanes) | ln] = u;
+        dst[(p1 << log_lanes) | ln] = w;
+    }
+}
+
+// cw[rep * N + i] = msg[i] for every replica (commit.rs:239-258).
+__global__ void replicate_fill(const uint4 *msg, uint4 *cw, uint64_t msg_words, int reps) {
+    for (uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; i < msg_words;
+         i += (uint64_t)gridDim.x * blockDim.x) {
+        const uint4 v = __ldcs(msg + i);
+        for (int r = 0; r < reps; ++r) __stcs(cw + (uint64_t)r * msg_words + i, v);
+    }
+}
+
+static inline unsigned grid_for(uint64_t n, int threads, int num_sms, int per_sm) {
+    uint64_t g = (n + threads - 1) / threads;
+    const uint64_t cap = (uint64_t)num_sms * per_sm;
+    if (g > cap) g = cap;
+    if (g < 1) g = 1;
+    return (unsigned)g;
+}
+
+static bool table_pass_ok(int ell, int layer, int layers, int log_lanes) {
+    // every CTA chunk (512 tasks) must lie inside one block B
+    const int log_task_per_b = ell - layer - layers + log_lanes;
+    return log_task_per_b >= 9;
+}
+
+static size_t table_smem(int layers) {
+    const int nt = layers == 2 ? 3 : 1;
+    return (size_t)nt * kT16Entries * 16 + (size_t)nt * 128 * 16;
+}
+
+void init_ntt_kernels() {
+    cudaFuncSetAttribute(ntt_table_pass<2>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                         (int)table_smem(2));
+    cudaFuncSetAttribute(ntt_table_pass<1>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                         (int)table_smem(1));
+}
+
+int launch_ntt(const Shape &s, uint32_t schedule, const uint4 *d_msg, uint4 *d_cw,
+               const uint4 *d_tw, cudaStream_t st, int num_sms, LaunchLog *log) {
+    auto mark = [&](const char *n) {
+        if (log) log->mark(n);
+    };
+    const int ell = s.k_code(), r = s.log_inv_rate, L = s.log_lanes, b = s.log_dim();
+    int launches = 0;
+    const uint4 *src = d_msg;
+    int src_bits = b;  // message positions are the low b bits of a codeword position
+    if (b == 0) {
+        replicate_fill<<<grid_for(s.msg_words(), 256, num_sms, 8), 256, 0, st>>>(
+            d_msg, d_cw, s.msg_words(), 1 << r);
+        mark("replicate_fill");
+        return 1;
+    }
+    const bool generic = (schedule & SCHED_GENERIC) != 0;
+    if (generic) {
+        for (int layer = r; layer < ell; ++layer) {
+            const uint64_t n_tasks = ((uint64_t)1 << (ell - 1)) << L;
+            ntt_generic_layer<<<grid_for(n_tasks, 256, num_sms, 8), 256, 0, st>>>(
+                src, d_cw, d_tw, ell, layer, L, src_bits, n_tasks);
+            mark("ntt_generic_layer");
+            ++launches;
+            src = d_cw;
+            src_bits = 62;
+        }
+        return launches;
+    }
+    int deep = (int)(schedule & SCHED_DEEP_MASK);
+    if (deep > b) deep = b;
+    if (deep > 4) deep = 4;
+    const bool radix2 = (schedule & SCHED_RADIX2) != 0;
+    int layer = r;
+    const int table_end = ell - deep;
+    while (layer < table_end) {
+        const int layers = (!radix2 && layer + 1 < table_end) ? 2 : 1;
+        if (!table_pass_ok(ell, layer, layers, L)) {
+            // too few tasks per block for table passes: generic single layers
+            const uint64_t n_tasks = ((uint64_t)1 << (ell - 1)) << L;
+            ntt_generic_layer<<<grid_for(n_tasks, 256, num_sms, 8), 256, 0, st>>>(
+                src, d_cw, d_tw, ell, layer, L, src_bits, n_tasks);
+            mark("ntt_generic_layer");
+            ++launches;
+            src = d_cw;
+            src_bits = 62;
+            layer += 1;
+            continue;
+        }
+        TablePassArgs a;
+        a.src = src;
+        a.dst = d_cw;
+        a.tw = d_tw;
+        a.ell = ell;
+        a.layer = layer;
+        a.log_lanes = L;
+        a.src_pos_bits = src_bits;
+        a.n_tasks = ((uint64_t)1 << (ell - layers)) << L;
+        const unsigned grid = (unsigned)std::min<uint64_t>(num_sms, a.n_tasks / 512);
+        if (layers == 2)
+            ntt_table_pass<2><<<grid, 512, table_smem(2), st>>>(a);
+        else
+            ntt_table_pass<1><<<grid, 512, table_smem(1), st>>>(a);
+        mark(layers == 2 ? (src == d_msg ? "ntt_table_pass2_first" : "ntt_table_pass2")
+                         : (src == d_msg ? "ntt_table_pass1_first" : "ntt_table_pass1"));
+        ++launches;
+        src = d_cw;
+        src_bits = 62;
+        layer += layers;
+    }
+    if (deep > 0) {
+        DeepArgs a;
+        a.src = src;
+        a.dst = d_cw;
+        a.tw = d_tw;
+        a.ell = ell;
+        a.log_lanes = L;
+        a.src_pos_bits = src_bits;
+        a.n_tasks = ((uint64_t)1 << (ell - deep)) << L;
+        const unsigned grid = grid_for(a.n_tasks, 256, num_sms, 8);
+        switch (deep) {
+            case 1: ntt_deep_pass<1><<<grid, 256, 0, st>>>(a); break;
+            case 2: ntt_deep_pass<2><<<grid, 256, 0, st>>>(a); break;
+            case 3: ntt_deep_pass<3><<<grid, 256, 0, st>>>(a); break;
+            default: ntt_deep_pass<4><<<grid, 256, 0, st>>>(a); break;
+        }
+        mark("ntt_deep_pass");
+        ++launches;
+    }
+    return launches;
+}
+
+}  // namespace bz

@@ -1,0 +1,61 @@
+// Definitions of the opaque ABI handles and helpers shared by the host
+// runtime translation units.
+#pragma once
+#include <cuda_runtime.h>
+
+#include <atomic>
+#include <map>
+#include <mutex>
+#include <set>
+#include <string>
+
+#include "../../include/bitz_gpu.h"
+#include "bz_internal.h"
+
+struct bz_commitment {
+    bz_ctx *ctx = nullptr;
+    bz::Shape shape;
+    uint4 *d_cw = nullptr;
+    uint8_t *d_tree = nullptr;
+    size_t cw_bytes = 0, tree_bytes = 0;
+    bool root_ready = false;
+    uint8_t root[32] = {0};
+};
+
+struct bz_ctx {
+    int device = 0;
+    int num_sms = 0;
+    cudaStream_t stream = nullptr;
+    uint64_t budget = 0;
+    std::atomic<uint64_t> in_use{0};
+    std::atomic<uint64_t> launches{0};
+    std::mutex err_mu, tw_mu, sched_mu, live_mu;
+    std::string last_error;
+    std::map<int, const uint4 *> twiddles;  // by k_code
+    std::map<uint64_t, uint32_t> schedules;  // by shape key
+    std::set<bz_commitment *> live;
+    uint8_t *scratch = nullptr;
+    size_t scratch_bytes = 0;
+    void *h_small = nullptr;  // 4 KiB pinned
+    void *d_small = nullptr;  // 4 KiB device
+    cudaEvent_t ev0 = nullptr, ev1 = nullptr;
+};
+
+namespace bz {
+inline uint64_t shape_key(const Shape &s) {
+    return (uint64_t)s.log_msg_len | ((uint64_t)s.log_inv_rate << 8) |
+           ((uint64_t)s.log_lanes << 16) | ((uint64_t)s.hash_kind << 24);
+}
+int set_err(bz_ctx *ctx, int code, const char *what, cudaError_t e);
+int set_msg(bz_ctx *ctx, int code, const std::string &msg);
+int shape_from_params(const bz_params *p, Shape &s, size_t n_words, std::string &why);
+int dev_alloc(bz_ctx *ctx, size_t bytes, void **p, bool budgeted);
+void dev_free(bz_ctx *ctx, void *p, size_t bytes, bool budgeted);
+int ensure_scratch(bz_ctx *ctx, size_t bytes);
+int get_twiddles(bz_ctx *ctx, int ell, const uint4 **out);
+uint32_t schedule_for(bz_ctx *ctx, const Shape &s);
+int alloc_commitment(bz_ctx *ctx, const Shape &s, bz_commitment **out);
+int enqueue_commit(bz_ctx *ctx, const Shape &s, const uint4 *d_msg, bz_commitment *c,
+                   cudaStream_t st, uint32_t schedule);
+int fetch_root(bz_commitment *c);
+}  // namespace bz

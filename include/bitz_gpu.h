@@ -1,0 +1,193 @@
+/*
+ * bitz_gpu.h -- C ABI of the GB300 (sm_103a) Ligerito / Reed-Solomon
+ * commitment library.
+ *
+ * Every entry point returns a bz_status code; nothing unwinds across the ABI.
+ * Buffers are plain pointers and sizes.  GF(2^128) elements are two
+ * little-endian uint64 words {lo, hi} (the reference's repr(C) Gf128,
+ * vendor/field/src/gf128.rs:91-96), so an array of n elements is uint64_t[2n]
+ * and its byte image is the reference's codeword byte view
+ * (flock-core/src/pcs/commit.rs:284-292).
+ *
+ * Reference paths are relative to the BitZ-PoC project root; "flock-core/"
+ * abbreviates vendor/flock-mod/crates/flock-core/.
+ */
+#ifndef BITZ_GPU_H
+#define BITZ_GPU_H
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define BZ_ABI_VERSION 1
+
+typedef enum {
+    BZ_OK = 0,
+    BZ_ERR_ARG = 1,      /* null pointer, bad size, bad enum */
+    BZ_ERR_SHAPE = 2,    /* the reference's PcsParams::validate / commit asserts */
+    BZ_ERR_CUDA = 3,     /* a CUDA runtime call failed (bz_last_error has text) */
+    BZ_ERR_NOMEM = 4,    /* device allocation failed or the memory budget is exceeded */
+    BZ_ERR_BUSY = 5,     /* server queue full */
+    BZ_ERR_TIMEOUT = 6,  /* a bounded wait ran out */
+    BZ_ERR_STATE = 7,    /* handle in the wrong state (e.g. opened twice, freed) */
+    BZ_ERR_NOTFOUND = 8  /* unknown request id */
+} bz_status;
+
+/* Merkle hash (flock-core/src/hash.rs:21-27; merkle.rs:203-232). */
+typedef enum { BZ_HASH_SHA256 = 0, BZ_HASH_BLAKE3 = 1 } bz_hash_kind;
+
+/* flock-core PcsParams (commit.rs:31-137) expressed in the packed domain:
+ *   log_msg_len    = m - LOG_PACKING (m - 7)
+ *   log_inv_rate   = r  (>= 1)
+ *   log_batch_size = log2 of the interleaved lanes (<= log_msg_len)
+ * Derived: log_dim = log_msg_len - log_batch_size, k_code = log_dim + r,
+ * n_leaves = 2^k_code, leaf bytes = 16 << log_batch_size. */
+typedef struct {
+    uint32_t log_msg_len;
+    uint32_t log_inv_rate;
+    uint32_t log_batch_size;
+    uint32_t hash_kind; /* bz_hash_kind */
+} bz_params;
+
+typedef struct bz_ctx bz_ctx;
+typedef struct bz_commitment bz_commitment; /* device-resident ProverData + root */
+
+/* ---- context ---------------------------------------------------------- */
+const char *bz_status_string(int status);
+/* Last error text recorded on this context (never NULL). */
+const char *bz_last_error(const bz_ctx *ctx);
+int bz_abi_version(void);
+/* One context per device.  mem_budget_bytes caps what the context keeps on
+ * the device for commitments and scratch (0 = 90 % of free memory). */
+int bz_ctx_create(int device, uint64_t mem_budget_bytes, bz_ctx **out);
+int bz_ctx_destroy(bz_ctx *ctx);
+/* The cudaStream_t every entry point of this context enqueues on. */
+void *bz_ctx_stream(bz_ctx *ctx);
+int bz_ctx_synchronize(bz_ctx *ctx);
+/* Bytes currently held by live commitments and scratch; budget. */
+int bz_ctx_memory(const bz_ctx *ctx, uint64_t *in_use, uint64_t *budget);
+/* Device allocation helpers for callers that hold no other CUDA runtime. */
+int bz_device_alloc(bz_ctx *ctx, size_t bytes, void **dptr);
+int bz_device_free(bz_ctx *ctx, void *dptr);
+int bz_memcpy_h2d(bz_ctx *ctx, void *dst, const void *src, size_t bytes);
+int bz_memcpy_d2h(bz_ctx *ctx, void *dst, const void *src, size_t bytes);
+int bz_host_alloc_pinned(size_t bytes, void **hptr);
+int bz_host_free_pinned(void *hptr);
+/* Stream-ordered timing on the context stream: begin records an event, end
+ * records a second one, synchronizes, and returns the elapsed milliseconds. */
+int bz_timer_begin(bz_ctx *ctx);
+int bz_timer_end(bz_ctx *ctx, float *ms);
+/* Number of this library's kernels enqueued on the context so far. */
+uint64_t bz_kernel_launches(const bz_ctx *ctx);
+
+/* ---- commit ------------------------------------------------------------ */
+/* Replaces flock_core::pcs::commit::commit(z_packed, params) -> (Commitment,
+ * ProverData)  (flock-core/src/pcs/commit.rs:180-200; commit_into :209-232;
+ * finalize_commit :262-315), reached from BitZ through BinaryPcs::commit
+ * (src/binary_pcs.rs:313-318) and commit_rs_flock_from_rows
+ * (src/ligerito_flock.rs:198-245).
+ * `msg` is host memory of n_words = 2^log_msg_len elements, laid out
+ * msg[col * 2^log_batch_size + lane].  The codeword and Merkle tree stay on
+ * the device inside *out until bz_commitment_free.  root receives the 32-byte
+ * Merkle root (Commitment::root).  Synchronous. */
+int bz_commit(bz_ctx *ctx, const uint64_t *msg, size_t n_words, const bz_params *params,
+              bz_commitment **out, uint8_t root[32]);
+/* Same, with the message already in device memory (no host copies). */
+int bz_commit_device(bz_ctx *ctx, const uint64_t *d_msg, size_t n_words,
+                     const bz_params *params, bz_commitment **out, uint8_t root[32]);
+/* Enqueue only: no synchronization, root readable after bz_ctx_synchronize
+ * through bz_commitment_root.  Used by graph capture and the benchmark. */
+int bz_commit_device_async(bz_ctx *ctx, const uint64_t *d_msg, size_t n_words,
+                           const bz_params *params, bz_commitment **out);
+int bz_commitment_root(bz_commitment *c, uint8_t root[32]);
+int bz_commitment_params(const bz_commitment *c, bz_params *params);
+/* Device pointers of the resident codeword (2^(k_code+log_batch_size)
+ * elements, cw[pos * lanes + lane]) and flat tree ((2 n_leaves - 1) * 32 B,
+ * leaves first, root last -- flock-core/src/merkle.rs:15-22). */
+int bz_commitment_device_ptrs(const bz_commitment *c, const uint64_t **d_codeword,
+                              const uint8_t **d_tree);
+int bz_commitment_copy_codeword(bz_commitment *c, uint64_t *out, size_t n_words);
+int bz_commitment_copy_tree(bz_commitment *c, uint8_t *out, size_t n_nodes);
+/* Opened rows for sorted query positions: out[i] = the 2^log_batch_size
+ * lanes at position positions[i] (the open_initial row gather of
+ * flock-core/src/pcs/ligerito.rs:3472-3482). */
+int bz_commitment_rows(bz_commitment *c, const uint64_t *positions, size_t q, uint64_t *out);
+/* merkle_multi_proof (flock-core/src/merkle.rs:688-741): sibling hashes in
+ * the reference's bottom-up sorted order; *n_hashes receives the count.
+ * out must hold cap hashes. */
+int bz_commitment_multiproof(bz_commitment *c, const uint64_t *positions, size_t q,
+                             uint8_t *out, size_t cap, size_t *n_hashes);
+int bz_commitment_free(bz_commitment *c);
+
+/* Phase timing: one commit as bz_commit_device with a CUDA event after every
+ * kernel; ms[i] is the device time of launch i and names + 32*i its kernel
+ * name (NUL terminated).  At most cap entries; *count receives the number of
+ * launches.  The commitment is freed before returning. */
+int bz_commit_profile(bz_ctx *ctx, const uint64_t *d_msg, size_t n_words,
+                      const bz_params *params, size_t cap, float *ms, char *names,
+                      size_t *count, uint8_t root[32]);
+
+/* ligero_commit (flock-core/src/pcs/ligerito.rs:2390-2434): the recursive
+ * levels' commit -- same replicate + NTT + Merkle over `poly` of
+ * 2^(log_msg_cols + log_num_interleaved) elements (device pointer). */
+int bz_ligero_commit_device(bz_ctx *ctx, const uint64_t *d_poly, uint32_t log_msg_cols,
+                            uint32_t log_num_interleaved, uint32_t log_inv_rate,
+                            uint32_t hash_kind, bz_commitment **out, uint8_t root[32]);
+
+/* ---- batched commit ----------------------------------------------------- */
+/* count independent commits (device messages) recorded into one CUDA graph
+ * and launched once; roots is count*32 bytes.  With use_graph = 0 the same
+ * work is issued as plain per-polynomial launches (the comparison path). */
+int bz_commit_batch_device(bz_ctx *ctx, size_t count, const uint64_t *const *d_msgs,
+                           const bz_params *params, bz_commitment **outs, uint8_t *roots,
+                           int use_graph);
+
+/* ---- sumcheck folds (device buffers) ------------------------------------ */
+/* fold_and_msg_lsb (flock-core/src/pcs/ligerito.rs:2634-2735), used by
+ * SumcheckProver::fold (:3046-3057): nf[j] = f[2j] + (f[2j]+f[2j+1])*r (same
+ * for b) and the next-round message (u0, u2) over the folded arrays. */
+int bz_fold_and_msg_lsb(bz_ctx *ctx, const uint64_t *d_f, const uint64_t *d_b, size_t n,
+                        const uint64_t r[2], uint64_t *d_nf, uint64_t *d_nb, uint64_t u0[2],
+                        uint64_t u2[2]);
+/* round_msg_lsb (ligerito.rs:2500-2537). */
+int bz_round_msg_lsb(bz_ctx *ctx, const uint64_t *d_f, const uint64_t *d_b, size_t n,
+                     uint64_t u0[2], uint64_t u2[2]);
+/* partial_eval_lsb (ligerito.rs:1678-1695): fold the k LSB variables by
+ * rs[0..k) (host array of k elements); d_out holds n >> k elements. */
+int bz_partial_eval_lsb(bz_ctx *ctx, const uint64_t *d_in, size_t n, const uint64_t *rs,
+                        size_t k, uint64_t *d_out);
+
+/* ---- ring switch (BitZ src/ligerito.rs) --------------------------------- */
+/* build_eq_x_r_vec (src/poly/utils.rs:46-120) on the device: 2^k entries. */
+int bz_build_eq_lsb(bz_ctx *ctx, const uint64_t *point, size_t k, uint64_t *d_out);
+/* sv_fold_mfr (src/ligerito.rs:317-375): sv[j] = sum_y eq[y]*bit_j(P[y]);
+ * sv is a host array of 128 elements. */
+int bz_sv_fold(bz_ctx *ctx, const uint64_t *d_packed, const uint64_t *d_eq, size_t n,
+               uint64_t *sv);
+/* phi_byte_tables + phi_from_words (src/ligerito.rs:384-427):
+ * d_out[y] = sum_{u in bits(eq_hi[y])} eq_r2[u]; eq_r2 is a host array of
+ * 128 elements. */
+int bz_phi_from_words(bz_ctx *ctx, const uint64_t *d_eq_hi, size_t n, const uint64_t *eq_r2,
+                      uint64_t *d_out);
+
+/* ---- synthetic inputs --------------------------------------------------- */
+/* RFC 8439 ChaCha20 keystream words (key = seed LE u64 zero padded, nonce 0,
+ * counter from 0), word i = keystream bytes [16 i, 16 i + 16). */
+int bz_chacha_fill_device(bz_ctx *ctx, uint64_t seed, uint64_t first_word, uint64_t *d_out,
+                          size_t n_words);
+int bz_chacha_fill_host(uint64_t seed, uint64_t first_word, uint64_t *out, size_t n_words,
+                        int n_threads);
+
+/* ---- schedule autotuner ---------------------------------------------------- */
+/* Times the candidate NTT schedules for this shape and keeps the fastest for
+ * later commits of the same shape on this context. */
+int bz_autotune(bz_ctx *ctx, const bz_params *params, int reps, uint32_t *chosen);
+int bz_schedule_get(bz_ctx *ctx, const bz_params *params, uint32_t *schedule);
+int bz_schedule_set(bz_ctx *ctx, const bz_params *params, uint32_t schedule);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* BITZ_GPU_H */
