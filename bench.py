@@ -22,6 +22,8 @@ import sys
 import threading
 import time
 
+import numpy as np
+
 REPO = os.path.dirname(os.path.abspath(__file__))
 for _p in (REPO, os.path.join(REPO, "bitz-poc_gb300")):
     if _p not in sys.path:
@@ -203,6 +205,7 @@ def run_gpu(args, ws, rank, local):
     import ctypes
 
     msg = bz.DeviceArray.chacha(SEED + rank, 1 << LOG_N, ctx)
+    schedule = ctx.autotune(params, reps=2) if not args.no_autotune else ctx.schedule(params)
 
     def one_commit():
         h = ctypes.c_void_p()
@@ -247,6 +250,16 @@ def run_gpu(args, ws, rank, local):
     total_ms = sum(step_ms)
     total_ms = D.max(total_ms)
     value = ws * args.steps * (1 << LOG_N) / (total_ms / 1e3)
+
+    if args.only_commit:
+        if rank == 0:
+            print(json.dumps({"metric": METRIC, "value": value, "unit": UNIT, "log_n": LOG_N,
+                              "ms_per_step": total_ms / args.steps, "schedule": schedule,
+                              "root": root0.hex()}), flush=True)
+        msg.free()
+        ctx.close()
+        D.close()
+        return 0
 
     # ---- end to end through the C ABI with host buffers ----------------
     hp = ctypes.c_void_p()
@@ -302,6 +315,9 @@ def run_gpu(args, ws, rank, local):
         batch = None
         if not args.skip_batch:
             batch = _bench_batch(ctx, bz, L, _lib, args)
+        serve = None
+        if not args.skip_serve:
+            serve = _bench_serve(ctx, bz, args)
 
         # ---- CPU baseline (oracle, all host threads, one full commit) -----
         cpu = None
@@ -333,7 +349,7 @@ def run_gpu(args, ws, rank, local):
             "phases_ms": {k: round(v[1], 4) for k, v in agg.items()},
             "phase_share": {k: round(v[1] / total_phase, 4) for k, v in agg.items()},
             "clocks": clk, "gpu_launches": launches, "wall_s": wall,
-            "batched": batch, "cpu_baseline": cpu,
+            "schedule": schedule, "batched": batch, "serving": serve, "cpu_baseline": cpu,
         }
         print(json.dumps(out), flush=True)
     msg.free()
@@ -343,32 +359,133 @@ def run_gpu(args, ws, rank, local):
 
 
 def _bench_batch(ctx, bz, L, _lib, args):
+    """64 polynomials, log2 sizes uniform on [16, 24] (seed 3), square-ish
+    2^floor(n/2) x 2^ceil(n/2) matrices, rate 1/4: one CUDA-graph launch of a
+    batch plan (per-shape autotuned schedules, 4 parallel branches) against the
+    same 64 committed one at a time by the plain GPU path."""
     import numpy as np
 
     rng = np.random.default_rng(3)
-    sizes = rng.integers(16, 25, 64)
-    params = [bz.PcsParams(int(n) + 7, LOG_INV_RATE, int(n) // 2, HASH) for n in sizes]
-    msgs = [bz.DeviceArray.chacha(3000 + i, 1 << int(n), ctx) for i, n in enumerate(sizes)]
-    total = int(sum(1 << int(n) for n in sizes))
+    sizes = [int(x) for x in rng.integers(16, 25, 64)]
+    params = [bz.PcsParams(n + 7, LOG_INV_RATE, n // 2, HASH) for n in sizes]
+    for p in {(p.m, p.log_batch_size): p for p in params}.values():
+        ctx.autotune(p, reps=1)
+    msgs = [bz.DeviceArray.chacha(3000 + i, 1 << n, ctx) for i, n in enumerate(sizes)]
+    total = int(sum(1 << n for n in sizes))
+    reps = 5
     res = {}
-    for mode, graph in (("graph", True), ("plain", False)):
-        out = bz.commit_batch(msgs, params, use_graph=graph, ctx=ctx)  # warm-up
-        for _, pd in out:
-            pd.free()
+    for mode, graph, branches in (("graph", True, 4), ("stream_plan", False, 4)):
+        plan = bz.BatchPlan(msgs, params, use_graph=graph, n_branches=branches, ctx=ctx)
+        plan.launch()
+        plan.roots()
         ctx.synchronize()
-        t0 = time.perf_counter()
-        reps = 3
+        ctx.timer_begin()
         for _ in range(reps):
-            out = bz.commit_batch(msgs, params, use_graph=graph, ctx=ctx)
-            for _, pd in out:
-                pd.free()
-        ctx.synchronize()
-        dt = (time.perf_counter() - t0) / reps
-        res[mode] = {"value": total / dt, "ms": dt * 1e3}
+            plan.launch()
+        ms = ctx.timer_end() / reps
+        roots = plan.roots()
+        plan.close()
+        res[mode] = {"value": total / (ms / 1e3), "ms": ms}
+    # plain: one commit at a time through bz_commit_device (root read per commit)
+    import ctypes
+
+    def plain_once():
+        out = []
+        for m, p in zip(msgs, params):
+            c, pd = bz.commit(m, p, ctx)
+            out.append(c.root)
+            pd.free()
+        return out
+
+    plain_roots = plain_once()
+    assert plain_roots == roots, "batched roots differ from one-at-a-time roots"
+    ctx.synchronize()
+    ctx.timer_begin()
+    for _ in range(reps):
+        plain_once()
+    ms = ctx.timer_end() / reps
+    res["plain"] = {"value": total / (ms / 1e3), "ms": ms}
     for m in msgs:
         m.free()
-    return {"polys": 64, "total_elems": total, "unit": UNIT,
-            "log2_sizes": [int(x) for x in sizes], **res}
+    return {"polys": 64, "total_elems": total, "unit": UNIT, "log2_sizes": sizes,
+            "speedup_graph_vs_plain": res["plain"]["ms"] / res["graph"]["ms"], **res}
+
+
+def _geometric_sizes(rng, n, lo=14, hi=26, q=0.97):
+    ks = np.arange(lo, hi + 1)
+    w = q ** (ks - lo)
+    w /= w.sum()
+    return rng.choice(ks, size=n, p=w)
+
+
+def _bench_serve(ctx, bz, args):
+    """Poisson commit-then-open requests with log2 sizes from a truncated
+    geometric on [14, 26], admitted by free HBM (continuous batching); the
+    arrival rate is swept to saturation.  Reports throughput and p50/p99
+    commit-to-opened latency per rate."""
+    import numpy as np
+    from bitz_gb300 import serve as S
+
+    rng = np.random.default_rng(4)
+    n_req = args.serve_requests
+    sizes = _geometric_sizes(rng, n_req)
+    # pinned host messages: one buffer of the largest size, prefixes reused
+    import ctypes
+
+    from bitz_gb300 import _lib
+
+    L = _lib.lib()
+    max_n = 1 << int(sizes.max())
+    hp = ctypes.c_void_p()
+    _lib.check(None, L.bz_host_alloc_pinned(16 * max_n, ctypes.byref(hp)))
+    _lib.check(None, L.bz_chacha_fill_host(4, 0, hp, max_n, os.cpu_count() or 1))
+    total_elems = int(sum(1 << int(k) for k in sizes))
+    out = {"requests": n_req, "log2_size_mean": float(sizes.mean()), "unit": UNIT,
+           "sizes": "truncated geometric on [14,26], q=0.97", "rates": []}
+    # saturation throughput estimate from the plain path: elems/s ~ 3e9
+    for load in (0.3, 0.6, 0.9, 1.5):
+        lam = load * 3.0e9 / (total_elems / n_req)       # requests per second
+        arrivals = np.cumsum(rng.exponential(1.0 / lam, n_req))
+        with S.Server(ctx, n_slots=4) as srv:
+            ids = [None] * n_req
+            t0 = time.perf_counter()
+            done = 0
+            i = 0
+            pending = []
+            lat = []
+            while done < n_req:
+                now = time.perf_counter() - t0
+                while i < n_req and arrivals[i] <= now:
+                    k = int(sizes[i])
+                    ids[i] = srv.submit_commit_ptr(hp.value, 1 << k,
+                                                   bz.PcsParams(k + 7, 2, k // 2, 1))
+                    pending.append(i)
+                    i += 1
+                still = []
+                for j in pending:
+                    st = srv.state(ids[j])
+                    if st == S.COMMITTED:
+                        srv.submit_open(ids[j], [0, 1, 7])
+                        still.append(j)
+                    elif st == S.OPENED:
+                        t = srv.times(ids[j])
+                        lat.append((t[4] - t[0]) / 1e6)
+                        srv.release(ids[j])
+                        done += 1
+                    elif st == S.FAILED:
+                        raise RuntimeError("serving request failed")
+                    else:
+                        still.append(j)
+                pending = still
+                time.sleep(0.0002)
+            wall = time.perf_counter() - t0
+        lat.sort()
+        out["rates"].append({
+            "offered_load": load, "arrival_rate_per_s": lam, "throughput": total_elems / wall,
+            "p50_ms": lat[len(lat) // 2], "p99_ms": lat[min(len(lat) - 1, int(0.99 * len(lat)))],
+            "wall_s": wall})
+    L.bz_host_free_pinned(hp)
+    return out
 
 
 def main():
@@ -379,7 +496,18 @@ def main():
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--skip-cpu", action="store_true")
     ap.add_argument("--skip-batch", action="store_true")
+    ap.add_argument("--skip-serve", action="store_true")
+    ap.add_argument("--no-autotune", action="store_true")
+    ap.add_argument("--only-commit", action="store_true",
+                    help="time the device commit loop only (profiling runs)")
+    ap.add_argument("--log-n", type=int, default=None, help="override log2 elements")
+    ap.add_argument("--serve-requests", type=int, default=160)
     args = ap.parse_args()
+    if args.log_n is not None:
+        global LOG_N, LOG_LANES, MSG_BYTES
+        LOG_N = args.log_n
+        LOG_LANES = args.log_n // 2
+        MSG_BYTES = 16 << LOG_N
     ws, rank, local = _dist()
     if args.impl == "reference":
         return run_reference(args, ws, rank)

@@ -14,6 +14,7 @@ from .pcs import (  # noqa: F401
     LigeroWitness,
     PcsParams,
     ProverData,
+    BatchPlan,
     chacha_words,
     commit,
     commit_batch,

@@ -360,3 +360,62 @@ def chacha_words(seed: int, n: int, first_word: int = 0, n_threads: int = 0) -> 
     check(None, lib().bz_chacha_fill_host(seed, first_word, ptr(out), n,
                                           n_threads or (os.cpu_count() or 1)))
     return out
+
+
+class BatchPlan:
+    """Reusable batched commit (bz_batch_plan_*): resident buffers for every
+    polynomial and, with ``use_graph``, one CUDA graph holding all kernels,
+    spread over ``n_branches`` parallel branches."""
+
+    def __init__(self, msgs, params_list, use_graph: bool = True, n_branches: int = 4,
+                 ctx: Context | None = None):
+        self.ctx = ctx or default_context()
+        L = lib()
+        for name, res, args in (
+                ("bz_batch_plan_create", ctypes.c_int,
+                 [ctypes.c_void_p, ctypes.c_size_t, ctypes.c_void_p, ctypes.POINTER(Params),
+                  ctypes.c_int, ctypes.c_int, ctypes.POINTER(ctypes.c_void_p)]),
+                ("bz_batch_plan_launch", ctypes.c_int, [ctypes.c_void_p]),
+                ("bz_batch_plan_roots", ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p]),
+                ("bz_batch_plan_commitment", ctypes.c_void_p, [ctypes.c_void_p, ctypes.c_size_t]),
+                ("bz_batch_plan_destroy", ctypes.c_int, [ctypes.c_void_p])):
+            f = getattr(L, name)
+            f.restype, f.argtypes = res, args
+        self.L = L
+        self.n = len(msgs)
+        self.params = list(params_list)
+        self._msgs = msgs
+        arr = (ctypes.c_void_p * self.n)(*[m.ptr.value if hasattr(m.ptr, "value") else m.ptr
+                                           for m in msgs])
+        ps = (Params * self.n)(*[p.to_c() for p in self.params])
+        h = ctypes.c_void_p()
+        check(self.ctx.handle, L.bz_batch_plan_create(self.ctx.handle, self.n, arr, ps,
+                                                      1 if use_graph else 0, n_branches,
+                                                      ctypes.byref(h)))
+        self.h = h
+
+    def launch(self):
+        check(self.ctx.handle, self.L.bz_batch_plan_launch(self.h))
+
+    def roots(self) -> list[bytes]:
+        out = np.zeros((self.n, 32), np.uint8)
+        check(self.ctx.handle, self.L.bz_batch_plan_roots(self.h, ptr(out)))
+        return [out[i].tobytes() for i in range(self.n)]
+
+    def codeword(self, i: int) -> np.ndarray:
+        c = self.L.bz_batch_plan_commitment(self.h, i)
+        n = self.params[i].codeword_len_f128()
+        out = np.zeros((n, 2), np.uint64)
+        check(self.ctx.handle, lib().bz_commitment_copy_codeword(c, ptr(out), n))
+        return out
+
+    def close(self):
+        if self.h:
+            self.L.bz_batch_plan_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass

@@ -238,3 +238,179 @@ int bz_autotune(bz_ctx *ctx, const bz_params *params, int reps, uint32_t *chosen
 }
 
 }  // extern "C"
+
+// ===========================================================================
+// Reusable batch plans.
+// ===========================================================================
+struct bz_batch_plan {
+    bz_ctx *ctx = nullptr;
+    std::vector<bz::Shape> shapes;
+    std::vector<const uint4 *> msgs;
+    std::vector<bz_commitment *> commits;
+    std::vector<uint32_t> schedules;
+    uint8_t *d_roots = nullptr;
+    int use_graph = 0;
+    int n_branches = 1;
+    std::vector<cudaStream_t> branches;
+    std::vector<cudaEvent_t> fork_join;  // [0] fork, [1..n] joins
+    cudaGraph_t graph = nullptr;
+    cudaGraphExec_t exec = nullptr;
+};
+
+namespace {
+
+// Enqueue every commit of the plan: polynomials are dealt to the branch
+// streams largest first (longest-processing-time), forked from and joined back
+// into the context stream.
+int plan_enqueue(bz_batch_plan *p) {
+    bz_ctx *ctx = p->ctx;
+    cudaStream_t main = ctx->stream;
+    const int nb = p->n_branches;
+    cudaEventRecord(p->fork_join[0], main);
+    for (int b = 0; b < nb; ++b) cudaStreamWaitEvent(p->branches[b], p->fork_join[0], 0);
+    std::vector<size_t> order(p->shapes.size());
+    for (size_t i = 0; i < order.size(); ++i) order[i] = i;
+    std::sort(order.begin(), order.end(), [&](size_t a, size_t b) {
+        return p->shapes[a].cw_words() > p->shapes[b].cw_words();
+    });
+    std::vector<double> load(nb, 0.0);
+    int rc = BZ_OK;
+    for (size_t i : order) {
+        const int b = (int)(std::min_element(load.begin(), load.end()) - load.begin());
+        load[b] += (double)p->shapes[i].cw_words();
+        cudaStream_t st = p->branches[b];
+        rc = enqueue_commit(ctx, p->shapes[i], p->msgs[i], p->commits[i], st, p->schedules[i]);
+        if (rc) break;
+        const uint8_t *src = p->commits[i]->d_tree + (p->shapes[i].tree_nodes() - 1) * 32;
+        cudaMemcpyAsync(p->d_roots + 32 * i, src, 32, cudaMemcpyDeviceToDevice, st);
+    }
+    for (int b = 0; b < nb; ++b) {
+        cudaEventRecord(p->fork_join[1 + b], p->branches[b]);
+        cudaStreamWaitEvent(main, p->fork_join[1 + b], 0);
+    }
+    return rc;
+}
+
+}  // namespace
+
+extern "C" {
+
+int bz_batch_plan_destroy(bz_batch_plan *p) {
+    if (!p) return BZ_ERR_ARG;
+    bz_ctx *ctx = p->ctx;
+    cudaStreamSynchronize(ctx->stream);
+    if (p->exec) cudaGraphExecDestroy(p->exec);
+    if (p->graph) cudaGraphDestroy(p->graph);
+    for (auto *c : p->commits)
+        if (c) bz_commitment_free(c);
+    if (p->d_roots) dev_free(ctx, p->d_roots, 0, false);
+    for (auto s : p->branches) cudaStreamDestroy(s);
+    for (auto e : p->fork_join) cudaEventDestroy(e);
+    cudaStreamSynchronize(ctx->stream);
+    delete p;
+    return BZ_OK;
+}
+
+int bz_batch_plan_create(bz_ctx *ctx, size_t count, const uint64_t *const *d_msgs,
+                         const bz_params *params, int use_graph, int n_branches,
+                         bz_batch_plan **out) {
+    if (!ctx || !d_msgs || !params || !out || count == 0) return BZ_ERR_ARG;
+    *out = nullptr;
+    bz_batch_plan *p = new bz_batch_plan();
+    p->ctx = ctx;
+    p->use_graph = use_graph;
+    p->n_branches = std::max(1, std::min(n_branches, 16));
+    p->shapes.resize(count);
+    int rc = BZ_OK;
+    size_t scratch = 0;
+    for (size_t i = 0; i < count && rc == BZ_OK; ++i) {
+        std::string why;
+        if (!d_msgs[i]) rc = set_msg(ctx, BZ_ERR_ARG, "null message");
+        if (rc == BZ_OK) {
+            rc = shape_from_params(&params[i], p->shapes[i], (size_t)1 << params[i].log_msg_len,
+                                   why);
+            if (rc) set_msg(ctx, rc, why);
+        }
+        if (rc == BZ_OK && merkle_scratch_bytes(p->shapes[i]) > 0 && p->n_branches > 1)
+            rc = set_msg(ctx, BZ_ERR_SHAPE,
+                         "leaves above 256 chunks need the shared scratch: use one branch");
+        if (rc == BZ_OK) {
+            const uint4 *tw = nullptr;
+            rc = get_twiddles(ctx, p->shapes[i].k_code(), &tw);
+        }
+        if (rc == BZ_OK) {
+            scratch = std::max(scratch, merkle_scratch_bytes(p->shapes[i]));
+            p->msgs.push_back((const uint4 *)d_msgs[i]);
+            p->schedules.push_back(schedule_for(ctx, p->shapes[i]));
+            bz_commitment *c = nullptr;
+            rc = alloc_commitment(ctx, p->shapes[i], &c);
+            p->commits.push_back(c);
+        }
+    }
+    if (rc == BZ_OK && scratch) rc = ensure_scratch(ctx, scratch);
+    if (rc == BZ_OK) rc = dev_alloc(ctx, count * 32, (void **)&p->d_roots, false);
+    if (rc == BZ_OK) {
+        p->branches.resize(p->n_branches);
+        p->fork_join.resize(p->n_branches + 1);
+        for (auto &s : p->branches) cudaStreamCreateWithFlags(&s, cudaStreamNonBlocking);
+        for (auto &e : p->fork_join) cudaEventCreateWithFlags(&e, cudaEventDisableTiming);
+        cudaStreamSynchronize(ctx->stream);
+    }
+    if (rc == BZ_OK && use_graph) {
+        cudaError_t e = cudaStreamBeginCapture(ctx->stream, cudaStreamCaptureModeThreadLocal);
+        if (e != cudaSuccess) rc = set_err(ctx, BZ_ERR_CUDA, "begin capture", e);
+        if (rc == BZ_OK) {
+            rc = plan_enqueue(p);
+            e = cudaStreamEndCapture(ctx->stream, &p->graph);
+            if (rc == BZ_OK && e != cudaSuccess) rc = set_err(ctx, BZ_ERR_CUDA, "end capture", e);
+        }
+        if (rc == BZ_OK) {
+            e = cudaGraphInstantiate(&p->exec, p->graph, 0);
+            if (e != cudaSuccess) rc = set_err(ctx, BZ_ERR_CUDA, "instantiate", e);
+        }
+        if (rc == BZ_OK) {
+            e = cudaGraphUpload(p->exec, ctx->stream);
+            if (e != cudaSuccess) rc = set_err(ctx, BZ_ERR_CUDA, "upload", e);
+        }
+    }
+    if (rc != BZ_OK) {
+        cudaGetLastError();
+        bz_batch_plan_destroy(p);
+        return rc;
+    }
+    *out = p;
+    return BZ_OK;
+}
+
+int bz_batch_plan_launch(bz_batch_plan *p) {
+    if (!p) return BZ_ERR_ARG;
+    bz_ctx *ctx = p->ctx;
+    if (p->use_graph) {
+        cudaError_t e = cudaGraphLaunch(p->exec, ctx->stream);
+        if (e != cudaSuccess) return set_err(ctx, BZ_ERR_CUDA, "graph launch", e);
+        ctx->launches += 0;  // kernel count recorded at capture time
+        return BZ_OK;
+    }
+    return plan_enqueue(p);
+}
+
+int bz_batch_plan_roots(bz_batch_plan *p, uint8_t *roots) {
+    if (!p || !roots) return BZ_ERR_ARG;
+    bz_ctx *ctx = p->ctx;
+    const size_t n = p->commits.size();
+    cudaError_t e = cudaMemcpyAsync(roots, p->d_roots, n * 32, cudaMemcpyDeviceToHost, ctx->stream);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(ctx->stream);
+    if (e != cudaSuccess) return set_err(ctx, BZ_ERR_CUDA, "plan roots", e);
+    for (size_t i = 0; i < n; ++i) {
+        memcpy(p->commits[i]->root, roots + 32 * i, 32);
+        p->commits[i]->root_ready = true;
+    }
+    return BZ_OK;
+}
+
+bz_commitment *bz_batch_plan_commitment(bz_batch_plan *p, size_t i) {
+    if (!p || i >= p->commits.size()) return nullptr;
+    return p->commits[i];
+}
+
+}  // extern "C"

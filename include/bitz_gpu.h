@@ -144,6 +144,74 @@ int bz_commit_batch_device(bz_ctx *ctx, size_t count, const uint64_t *const *d_m
                            const bz_params *params, bz_commitment **outs, uint8_t *roots,
                            int use_graph);
 
+/* Reusable batch plan: the resident buffers of count commits and, with
+ * use_graph != 0, one CUDA graph holding every kernel of every commit (the
+ * polynomials spread over n_branches parallel branches so small ones overlap
+ * on the device).  Each launch recommits the same device messages (their
+ * contents may change between launches).  The shapes' NTT schedules are the
+ * context's (bz_autotune before creating the plan picks them per shape).
+ * This is the batched path of the reference's many-commit callers; there is
+ * no single reference function it replaces. */
+typedef struct bz_batch_plan bz_batch_plan;
+int bz_batch_plan_create(bz_ctx *ctx, size_t count, const uint64_t *const *d_msgs,
+                         const bz_params *params, int use_graph, int n_branches,
+                         bz_batch_plan **out);
+/* Enqueue one launch of the plan on the context stream (no synchronization). */
+int bz_batch_plan_launch(bz_batch_plan *plan);
+/* Synchronize and copy the count roots (count * 32 bytes). */
+int bz_batch_plan_roots(bz_batch_plan *plan, uint8_t *roots);
+/* The i-th commitment (owned by the plan; valid until the plan is destroyed). */
+bz_commitment *bz_batch_plan_commitment(bz_batch_plan *plan, size_t i);
+int bz_batch_plan_destroy(bz_batch_plan *plan);
+
+/* ---- serving: continuous-batching commit / open server ------------------- */
+/* A scheduler thread admits queued commits whenever one of n_slots execution
+ * slots (CUDA streams) is free and the request's device memory (message
+ * staging + resident codeword + tree) fits in mem_budget_bytes (0 = the
+ * context budget); later arrivals start as earlier ones finish or are opened,
+ * and their kernels overlap on the device.  Codewords and trees stay resident
+ * until opened.  The serving counterpart of the reference's
+ * commit-then-open flow (BinaryPcs::commit then open_*, src/binary_pcs.rs:
+ * 313-431); the reference has no server of its own. */
+typedef struct bz_server bz_server;
+enum {
+    BZ_REQ_QUEUED = 0,
+    BZ_REQ_RUNNING = 1,
+    BZ_REQ_COMMITTED = 2,
+    BZ_REQ_OPEN_QUEUED = 3,
+    BZ_REQ_OPENING = 4,
+    BZ_REQ_OPENED = 5,
+    BZ_REQ_FAILED = 6
+};
+int bz_server_create(bz_ctx *ctx, int n_slots, uint64_t mem_budget_bytes, size_t queue_cap,
+                     bz_server **out);
+/* host_msg must stay valid until the request reaches BZ_REQ_COMMITTED
+ * (pinned host memory gives overlapped copies).  BZ_ERR_BUSY when the queue
+ * holds queue_cap commits. */
+int bz_server_submit_commit(bz_server *s, const uint64_t *host_msg, size_t n_words,
+                            const bz_params *params, uint64_t *request_id);
+/* Queue an opening of a committed request at q positions: the opened rows
+ * and the multi-proof (merkle_multi_proof order); frees the resident
+ * codeword and tree when done. */
+int bz_server_submit_open(bz_server *s, uint64_t request_id, const uint64_t *positions,
+                          size_t q);
+int bz_server_poll(bz_server *s, uint64_t request_id, int *state);
+/* Wait (bounded by timeout_ms) until the request reaches target_state;
+ * BZ_ERR_TIMEOUT when the wait runs out. */
+int bz_server_wait(bz_server *s, uint64_t request_id, int target_state, uint32_t timeout_ms);
+int bz_server_root(bz_server *s, uint64_t request_id, uint8_t root[32]);
+/* rows: q * 2^log_batch_size elements for the sorted unique positions;
+ * proof: n_hashes * 32 bytes.  Either output may be NULL (size query). */
+int bz_server_open_result(bz_server *s, uint64_t request_id, uint64_t *rows,
+                          size_t rows_cap_words, uint8_t *proof, size_t proof_cap,
+                          size_t *n_rows, size_t *n_hashes);
+/* ns since server start: submit, start, committed, open submitted, opened */
+int bz_server_times(bz_server *s, uint64_t request_id, int64_t times[5]);
+int bz_server_release(bz_server *s, uint64_t request_id);
+int bz_server_stats(bz_server *s, uint64_t *committed, uint64_t *opened, uint64_t *failed,
+                    uint64_t *in_use, uint64_t *queued);
+int bz_server_destroy(bz_server *s);
+
 /* ---- sumcheck folds (device buffers) ------------------------------------ */
 /* fold_and_msg_lsb (flock-core/src/pcs/ligerito.rs:2634-2735), used by
  * SumcheckProver::fold (:3046-3057): nf[j] = f[2j] + (f[2j]+f[2j+1])*r (same

@@ -1,0 +1,111 @@
+"""Serving and batch plans: every result is the same alone and in the mix."""
+import threading
+import time
+
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+
+def _shapes(rng, n, lo=10, hi=18):
+    out = []
+    for _ in range(n):
+        k = int(rng.integers(lo, hi + 1))
+        out.append((k, k // 2))
+    return out
+
+
+def test_server_results_equal_alone_and_in_the_mix(oracle, ctx):
+    from bitz_gb300 import PcsParams, commit
+    from bitz_gb300.serve import COMMITTED, OPENED, Server
+
+    rng = np.random.default_rng(5)
+    shapes = _shapes(rng, 24)
+    msgs = [oracle.chacha_words(500 + i, 1 << k) for i, (k, _) in enumerate(shapes)]
+    params = [PcsParams(k + 7, 2, a, 1) for (k, a) in shapes]
+    queries = []
+    with Server(ctx, n_slots=4) as srv:
+        ids = []
+        for i, (m, p) in enumerate(zip(msgs, params)):
+            ids.append(srv.submit_commit(m, p))
+        for i, rid in enumerate(ids):
+            srv.wait(rid, COMMITTED, 120000)
+            n_leaves = params[i].n_leaves()
+            q = sorted(set(rng.integers(0, n_leaves, 9).tolist()))
+            queries.append(q)
+            srv.submit_open(rid, q)
+        for i, rid in enumerate(ids):
+            srv.wait(rid, OPENED, 120000)
+            root = srv.root(rid)
+            rows, proof = srv.open_result(rid, params[i].num_ntts())
+            # alone: the plain commit path and the oracle
+            c, pd = commit(msgs[i], params[i], ctx)
+            assert root == c.root
+            assert (rows == pd.rows(queries[i])).all()
+            assert (proof == pd.multi_proof(queries[i])).all()
+            pd.free()
+            srv.release(rid)
+        st = srv.stats()
+        assert st["committed"] == 24 and st["opened"] == 24 and st["failed"] == 0
+        assert st["in_use"] == 0
+
+
+def test_server_admission_by_memory(oracle, ctx):
+    """With a budget that holds one request, the second waits until the first
+    is opened (its codeword freed), then runs."""
+    from bitz_gb300 import PcsParams
+    from bitz_gb300.serve import COMMITTED, OPENED, QUEUED, Server
+
+    p = PcsParams(18 + 7, 2, 9, 1)
+    need = (16 << 18) + (16 << 20) + 32 * (2 * (1 << 11) - 1)
+    m1, m2 = oracle.chacha_words(1, 1 << 18), oracle.chacha_words(2, 1 << 18)
+    with Server(ctx, n_slots=4, mem_budget_bytes=int(need * 1.5)) as srv:
+        a = srv.submit_commit(m1, p)
+        srv.wait(a, COMMITTED, 60000)
+        b = srv.submit_commit(m2, p)
+        time.sleep(0.2)
+        assert srv.state(b) == QUEUED          # not admitted: memory held by a
+        srv.submit_open(a, [0, 5])
+        srv.wait(a, OPENED, 60000)
+        srv.wait(b, COMMITTED, 60000)          # admitted once a freed its HBM
+        _, _, root = oracle.commit(m2, 2, 9, 1)
+        assert srv.root(b) == root
+        srv.submit_open(b, [1])
+        srv.wait(b, OPENED, 60000)
+
+
+def test_server_bounded_wait_times_out(ctx):
+    from bitz_gb300 import BzError, PcsParams
+    from bitz_gb300.serve import OPENED, Server
+
+    with Server(ctx, n_slots=1) as srv:
+        m = np.zeros((1 << 12, 2), np.uint64)
+        rid = srv.submit_commit(m, PcsParams(12 + 7, 2, 6, 1))
+        with pytest.raises(BzError) as e:
+            srv.wait(rid, OPENED, 200)         # never opened: the wait must end
+        assert e.value.status == 6
+
+
+def test_batch_plan_matches_single(oracle, ctx):
+    from bitz_gb300 import BatchPlan, DeviceArray, PcsParams, commit
+
+    rng = np.random.default_rng(8)
+    shapes = _shapes(rng, 16, 12, 20)
+    params = [PcsParams(k + 7, 2, a, 1) for (k, a) in shapes]
+    msgs = [DeviceArray.chacha(70 + i, 1 << k, ctx) for i, (k, _) in enumerate(shapes)]
+    single = []
+    for m, p in zip(msgs, params):
+        c, pd = commit(m, p, ctx)
+        single.append((c.root, pd.codeword))
+        pd.free()
+    for graph in (True, False):
+        for branches in (1, 4):
+            plan = BatchPlan(msgs, params, use_graph=graph, n_branches=branches, ctx=ctx)
+            for _ in range(2):
+                plan.launch()
+            roots = plan.roots()
+            for i in range(len(msgs)):
+                assert roots[i] == single[i][0]
+                assert (plan.codeword(i) == single[i][1]).all()
+            plan.close()
