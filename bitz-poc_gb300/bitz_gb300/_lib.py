@@ -68,6 +68,7 @@ _SIGS = {
     "bz_ligero_commit_device": (_I, [_P, _P, _U32, _U32, _U32, _U32, _PP, _P]),
     "bz_commit_batch_device": (_I, [_P, _S, _P, ctypes.POINTER(Params), _PP, _P, _I]),
     "bz_fold_and_msg_lsb": (_I, [_P, _P, _P, _S, _P, _P, _P, _P, _P]),
+    "bz_fold_and_msg_lsb_static": (_I, [_P, _P, _S, _P, _P, _P, _P, _P]),
     "bz_round_msg_lsb": (_I, [_P, _P, _P, _S, _P, _P]),
     "bz_partial_eval_lsb": (_I, [_P, _P, _S, _P, _S, _P]),
     "bz_build_eq_lsb": (_I, [_P, _P, _S, _P]),

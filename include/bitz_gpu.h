@@ -219,6 +219,21 @@ int bz_server_destroy(bz_server *s);
 int bz_fold_and_msg_lsb(bz_ctx *ctx, const uint64_t *d_f, const uint64_t *d_b, size_t n,
                         const uint64_t r[2], uint64_t *d_nf, uint64_t *d_nb, uint64_t u0[2],
                         uint64_t u2[2]);
+/* Allocation-free bz_fold_and_msg_lsb, for callers that cannot allocate
+ * device memory (a host runtime that reserved the GPU's memory for its own
+ * pool, or a fold loop that cannot afford cudaMalloc's synchronisation).  No
+ * counterpart in the reference: it is the same fold with its per-block
+ * scratch in a fixed 64 KiB device array instead of allocated memory.  The
+ * caller passes device inputs/outputs and a stream (NULL = default stream) on
+ * the current device; d_msg receives {u0.lo, u0.hi, u2.lo, u2.hi} on the
+ * device.  Enqueue only: synchronize the stream before reading outputs.  n
+ * must be a power of two in [2, 2^40] (BZ_ERR_SHAPE otherwise).  The first
+ * call on each device resolves the array's device address; make it before any
+ * stream capture.  Calls that overlap on the GPU share the array and race.
+ * Allocates nothing (no cudaMalloc, cudaFree or allocating library call). */
+int bz_fold_and_msg_lsb_static(const uint64_t *d_f, const uint64_t *d_b, size_t n,
+                               const uint64_t r[2], uint64_t *d_nf, uint64_t *d_nb,
+                               uint64_t *d_msg, void *stream);
 /* round_msg_lsb (ligerito.rs:2500-2537). */
 int bz_round_msg_lsb(bz_ctx *ctx, const uint64_t *d_f, const uint64_t *d_b, size_t n,
                      uint64_t u0[2], uint64_t u2[2]);
