@@ -274,14 +274,38 @@ def run_gpu(args, ws, rank, local):
         L.bz_commitment_free(h)
         return bytes(root)
 
+    def e2e_submit():
+        h = ctypes.c_void_p()
+        _lib.check(ctx.handle, L.bz_commit_async(ctx.handle, hp, 1 << LOG_N, ctypes.byref(pc),
+                                                 ctypes.byref(h)))
+        return h
+
+    def e2e_finish(h):
+        root = (ctypes.c_uint8 * 32)()
+        _lib.check(ctx.handle, L.bz_commitment_root(h, root))
+        L.bz_commitment_free(h)
+        return bytes(root)
+
     assert e2e_commit() == root0
-    e2e_commit()
+    assert e2e_finish(e2e_submit()) == root0
+    # every step: H2D of its own 256 MiB message from pinned memory, the commit
+    # kernels and the D2H of its root; step i+1's upload overlaps step i's kernels
     D.barrier()
+    ctx.synchronize()
+    t_e2e0 = time.perf_counter()
+    prev = e2e_submit()
+    for _ in range(args.steps - 1):
+        nxt = e2e_submit()
+        assert e2e_finish(prev) == root0
+        prev = nxt
+    assert e2e_finish(prev) == root0
+    e2e_ms = D.max((time.perf_counter() - t_e2e0) * 1e3)
+    # the synchronous C-ABI call (no overlap) for reference
     ctx.synchronize()
     ctx.timer_begin()
     for _ in range(args.steps):
         e2e_commit()
-    e2e_ms = D.max(ctx.timer_end())
+    e2e_sync_ms = D.max(ctx.timer_end())
     e2e_value = ws * args.steps * (1 << LOG_N) / (e2e_ms / 1e3)
     L.bz_host_free_pinned(hp)
 
@@ -318,6 +342,12 @@ def run_gpu(args, ws, rank, local):
         serve = None
         if not args.skip_serve:
             serve = _bench_serve(ctx, bz, args)
+        shapes = None
+        if not args.skip_shapes:
+            shapes = _bench_shapes(ctx, bz)
+        opening = None
+        if not args.skip_open:
+            opening = _bench_open(ctx, bz, msg, params)
 
         # ---- CPU baseline (oracle, all host threads, one full commit) -----
         cpu = None
@@ -340,7 +370,9 @@ def run_gpu(args, ws, rank, local):
             "latency_ms": {"p50": statistics.median(step_ms), "p99": p99,
                            "min": sorted_ms[0], "max": sorted_ms[-1]},
             "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": MSG_BYTES,
-                    "d2h_bytes_per_step": 32},
+                    "d2h_bytes_per_step": 32, "api": "bz_commit_async + bz_commitment_root",
+                    "pipelined": "upload of step i+1 overlaps the kernels of step i",
+                    "sync_call_value": ws * args.steps * (1 << LOG_N) / (e2e_sync_ms / 1e3)},
             "roofline": {"bound": "hbm", "kernel": dom_name, "achieved": achieved, "peak": peak,
                          "unit": "GB/s", "frac": achieved / peak, "traffic": None,
                          "alg_bytes_per_launch": alg_bytes, "launch_ms": dom_ms / dom_n,
@@ -349,7 +381,8 @@ def run_gpu(args, ws, rank, local):
             "phases_ms": {k: round(v[1], 4) for k, v in agg.items()},
             "phase_share": {k: round(v[1] / total_phase, 4) for k, v in agg.items()},
             "clocks": clk, "gpu_launches": launches, "wall_s": wall,
-            "schedule": schedule, "batched": batch, "serving": serve, "cpu_baseline": cpu,
+            "schedule": schedule, "batched": batch, "serving": serve, "shapes": shapes,
+            "opening": opening, "cpu_baseline": cpu,
         }
         print(json.dumps(out), flush=True)
     msg.free()
@@ -409,6 +442,67 @@ def _bench_batch(ctx, bz, L, _lib, args):
         m.free()
     return {"polys": 64, "total_elems": total, "unit": UNIT, "log2_sizes": sizes,
             "speedup_graph_vs_plain": res["plain"]["ms"] / res["graph"]["ms"], **res}
+
+
+def _bench_shapes(ctx, bz):
+    """The 2^20-element (2^10 x 2^10) and 2^28-element (2^14 x 2^14, 16 GiB
+    codeword resident in HBM) commits at rate 1/4, BLAKE3; NTT and Merkle
+    phases timed separately (device events around every kernel)."""
+    out = {}
+    peak, _ = _peaks()
+    for log_n, reps in ((20, 10), (28, 3)):
+        p = bz.PcsParams(log_n + 7, LOG_INV_RATE, log_n // 2, HASH)
+        m = bz.DeviceArray.chacha(log_n, 1 << log_n, ctx)
+        sched = ctx.autotune(p, reps=1)
+        best = None
+        for _ in range(reps):
+            phases, root = ctx.commit_profile(m, p)
+            tot = sum(t for _, t in phases)
+            if best is None or tot < best[0]:
+                best = (tot, phases)
+        tot, phases = best
+        ntt = sum(t for n, t in phases if n.startswith("ntt") or n == "replicate_fill")
+        mk = tot - ntt
+        cw_bytes = 16 << (log_n + LOG_INV_RATE)
+        out[f"2^{log_n}"] = {
+            "value": (1 << log_n) / (tot / 1e3), "unit": UNIT, "ms": tot, "ntt_ms": ntt,
+            "merkle_ms": mk, "schedule": sched, "root": root.hex(),
+            "commit_alg_gbs": ALG_BYTES_PER_WORD * (1 << log_n) / (tot / 1e3) / 1e9,
+            "merkle_read_gbs": cw_bytes / (mk / 1e3) / 1e9, "hbm_peak_gbs": peak}
+        m.free()
+    return out
+
+
+def _bench_open(ctx, bz, msg, params):
+    """Opening leg at 2^24: the 12-round L0 lane fold of the committed
+    message against a basis polynomial (SumcheckProver.new + 12 folds), then
+    148 opened rows and their Merkle multi-proof from the resident commitment."""
+    import numpy as np
+    from bitz_gb300.ligerito import SumcheckProver
+
+    rng = np.random.default_rng(12)
+    b = bz.DeviceArray.chacha(77, msg.n, ctx)
+    c, pd = bz.commit(msg, params, ctx)
+    rs = rng.integers(0, 2**64, (12, 2), dtype=np.uint64)
+    q = sorted(set(rng.integers(0, params.n_leaves(), 148).tolist()))
+    times = []
+    for _ in range(3):
+        ctx.synchronize()
+        t0 = time.perf_counter()
+        prover, _ = SumcheckProver.new(msg, b, 0)
+        for r in rs:
+            prover.fold(r)
+        t1 = time.perf_counter()
+        rows = pd.rows(q)
+        proof = pd.multi_proof(q)
+        t2 = time.perf_counter()
+        times.append((t1 - t0, t2 - t1))
+    pd.free()
+    b.free()
+    fold_s, open_s = min(times)
+    return {"fold_12_rounds_ms": fold_s * 1e3, "queries": len(q),
+            "rows_and_multiproof_ms": open_s * 1e3, "proof_hashes": int(len(proof)),
+            "row_bytes": int(rows.nbytes)}
 
 
 def _geometric_sizes(rng, n, lo=14, hi=26, q=0.97):
@@ -497,6 +591,8 @@ def main():
     ap.add_argument("--skip-cpu", action="store_true")
     ap.add_argument("--skip-batch", action="store_true")
     ap.add_argument("--skip-serve", action="store_true")
+    ap.add_argument("--skip-shapes", action="store_true")
+    ap.add_argument("--skip-open", action="store_true")
     ap.add_argument("--no-autotune", action="store_true")
     ap.add_argument("--only-commit", action="store_true",
                     help="time the device commit loop only (profiling runs)")

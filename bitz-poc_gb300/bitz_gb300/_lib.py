@@ -55,6 +55,7 @@ _SIGS = {
     "bz_commit": (_I, [_P, _P, _S, ctypes.POINTER(Params), _PP, _P]),
     "bz_commit_device": (_I, [_P, _P, _S, ctypes.POINTER(Params), _PP, _P]),
     "bz_commit_device_async": (_I, [_P, _P, _S, ctypes.POINTER(Params), _PP]),
+    "bz_commit_async": (_I, [_P, _P, _S, ctypes.POINTER(Params), _PP]),
     "bz_commitment_root": (_I, [_P, _P]),
     "bz_commitment_params": (_I, [_P, ctypes.POINTER(Params)]),
     "bz_commitment_device_ptrs": (_I, [_P, _PP, _PP]),

@@ -106,6 +106,7 @@ int bz_commit_batch_device(bz_ctx *ctx, size_t count, const uint64_t *const *d_m
         int rc = ensure_scratch(ctx, scratch);
         if (rc) return rc;
     }
+    if (!get_aux(ctx, ctx->stream)) return set_msg(ctx, BZ_ERR_CUDA, "aux stream");
     void *d_roots = nullptr;
     int rc = dev_alloc(ctx, count * 32, &d_roots, false);
     if (rc) return rc;
@@ -201,8 +202,24 @@ int bz_autotune(bz_ctx *ctx, const bz_params *params, int reps, uint32_t *chosen
     std::vector<uint32_t> cands;
     const int b = s.log_dim();
     for (int d = 0; d <= std::min(4, b); ++d) {
-        cands.push_back((uint32_t)d);
-        cands.push_back((uint32_t)d | SCHED_RADIX2);
+        for (uint32_t r2 : {0u, (uint32_t)SCHED_RADIX2}) {
+            if (d == 0) {
+                cands.push_back(r2);
+                continue;
+            }
+            for (uint32_t mode = 0; mode < 3; ++mode) {
+                cands.push_back((uint32_t)d | r2 | (mode << SCHED_MODE_SHIFT));
+                if (s.log_lanes >= 9 && d <= 3)
+                    cands.push_back((uint32_t)d | r2 | SCHED_FUSED_TAIL |
+                                    (mode << SCHED_MODE_SHIFT));
+            }
+            cands.push_back((uint32_t)d | r2 | SCHED_PREFETCH);
+            cands.push_back((uint32_t)d | r2 | SCHED_PREFETCH | SCHED_SMALL_CTA);
+            for (uint32_t small : {0u, (uint32_t)SCHED_SMALL_CTA})
+                for (uint32_t pipe = 0; pipe < 4; ++pipe)
+                    if (small || pipe)
+                        cands.push_back((uint32_t)d | r2 | small | (pipe << SCHED_PIPE_SHIFT));
+        }
     }
     float best = 1e30f;
     uint32_t best_s = default_schedule(s);
@@ -355,6 +372,11 @@ int bz_batch_plan_create(bz_ctx *ctx, size_t count, const uint64_t *const *d_msg
         for (auto &s : p->branches) cudaStreamCreateWithFlags(&s, cudaStreamNonBlocking);
         for (auto &e : p->fork_join) cudaEventCreateWithFlags(&e, cudaEventDisableTiming);
         cudaStreamSynchronize(ctx->stream);
+    }
+    if (rc == BZ_OK) {
+        // auxiliary streams of pipelined schedules exist before any capture
+        for (auto st : p->branches)
+            if (!get_aux(ctx, st)) rc = set_msg(ctx, BZ_ERR_CUDA, "aux stream");
     }
     if (rc == BZ_OK && use_graph) {
         cudaError_t e = cudaStreamBeginCapture(ctx->stream, cudaStreamCaptureModeThreadLocal);

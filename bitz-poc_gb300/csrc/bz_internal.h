@@ -45,8 +45,19 @@ struct LaunchLog {
 // ---- NTT schedule ----------------------------------------------------------
 // Packed as: bits 0..3 = number of deep (shift-and-XOR) layers D (0..4),
 // bit 4 = use radix-2 passes only for the table layers, bit 5 = force the
-// generic one-layer-per-launch kernels (reference / fallback path).
-enum : uint32_t { SCHED_DEEP_MASK = 0xF, SCHED_RADIX2 = 0x10, SCHED_GENERIC = 0x20 };
+// generic one-layer-per-launch kernels (reference / fallback path), bit 6 =
+// fuse the last table layers with the deep layers into one tail pass, bits
+// 7..8 = narrow-multiply variant (0 shifts, 1 wide multiplies, 2 alternate).
+enum : uint32_t {
+    SCHED_DEEP_MASK = 0xF,
+    SCHED_RADIX2 = 0x10,
+    SCHED_GENERIC = 0x20,
+    SCHED_FUSED_TAIL = 0x40,
+    SCHED_MODE_SHIFT = 7,
+    SCHED_SMALL_CTA = 0x200,      // 256-thread table passes (room for co-resident CTAs)
+    SCHED_PIPE_SHIFT = 10,        // bits 10..11: log2 of the pipeline chunk count
+    SCHED_PREFETCH = 0x1000,      // radix-4 table passes double-buffer their loads
+};
 uint32_t default_schedule(const Shape &s);
 
 // Twiddle heap for AdditiveNttF128::standard(ell): tw[(1 << l) + b] =
@@ -57,6 +68,30 @@ std::vector<uint64_t> twiddle_heap(int ell);
 // fused (reads d_msg, writes d_cw).  Returns the number of kernels launched.
 int launch_ntt(const Shape &s, uint32_t schedule, const uint4 *d_msg, uint4 *d_cw,
                const uint4 *d_tw, cudaStream_t st, int num_sms, LaunchLog *log = nullptr);
+
+// Range-restricted NTT passes over positions [p0, p1) (aligned to the pass's
+// blocks), used by the pipelined commit.
+int launch_table_pass(const Shape &s, int layer, int layers, const uint4 *src, int src_bits,
+                      uint4 *dst, const uint4 *tw, uint64_t p0, uint64_t p1, int threads,
+                      cudaStream_t st, int num_sms, bool prefetch = false);
+int launch_deep_range(const Shape &s, int deep, int mode, const uint4 *src, int src_bits,
+                      uint4 *dst, const uint4 *tw, uint64_t p0, uint64_t p1, cudaStream_t st,
+                      int num_sms);
+// Leaf hashes of positions [p0, p1) (BLAKE3 leaves of <= 256 chunks, SHA-256)
+// and the parent levels above all leaves.
+bool leaves_range_supported(const Shape &s);
+int launch_leaves_range(const Shape &s, const uint4 *d_cw, uint8_t *d_tree, uint64_t p0,
+                        uint64_t p1, cudaStream_t st);
+int launch_merkle_levels(const Shape &s, uint8_t *d_tree, cudaStream_t st, LaunchLog *log);
+// Two-stream software pipeline of one commit: after the first table pass,
+// position chunks go through the remaining table passes on `st` while the
+// previous chunk's deep layers and leaf hashes run on `aux` (the two kinds of
+// kernels bind different units and share SMs).  `ev` holds >= chunks + 2
+// events.  Returns kernels launched, or -1 when the shape/schedule does not
+// pipeline (the caller then uses launch_ntt + launch_merkle).
+int launch_commit_pipelined(const Shape &s, uint32_t schedule, const uint4 *d_msg, uint4 *d_cw,
+                            uint8_t *d_tree, const uint4 *d_tw, cudaStream_t st,
+                            cudaStream_t aux, cudaEvent_t *ev, int num_sms, LaunchLog *log);
 
 // Merkle tree over the codeword rows (leaves = positions).  d_scratch must hold
 // merkle_scratch_bytes(s).  Returns kernels launched.

@@ -9,19 +9,24 @@ namespace bz {
 
 __device__ __constant__ uint32_t kIV[8] = {0x6A09E667u, 0xBB67AE85u, 0x3C6EF372u, 0xA54FF53Au,
                                            0x510E527Fu, 0x9B05688Cu, 0x1F83D9ABu, 0x5BE0CD19u};
+__device__ __constant__ uint32_t kOne = 1;
 constexpr uint32_t B3_CHUNK_START = 1, B3_CHUNK_END = 2, B3_PARENT = 4, B3_ROOT = 8;
 
 __device__ __forceinline__ uint32_t rotr(uint32_t x, int n) { return __funnelshift_r(x, x, n); }
 
+// The two c += d additions are written as multiply-adds by a runtime 1
+// (`one`, read from constant memory so the compiler cannot fold it): they
+// then issue on the FMA pipe instead of the ALU pipe, which BLAKE3's xors and
+// rotates otherwise saturate.
 #define BZ_B3G(a, b, c, d, x, y)          \
     do {                                  \
         s##a = s##a + s##b + (x);         \
         s##d = rotr(s##d ^ s##a, 16);     \
-        s##c = s##c + s##d;               \
+        s##c = s##d * one + s##c;         \
         s##b = rotr(s##b ^ s##c, 12);     \
         s##a = s##a + s##b + (y);         \
         s##d = rotr(s##d ^ s##a, 8);      \
-        s##c = s##c + s##d;               \
+        s##c = s##d * one + s##c;         \
         s##b = rotr(s##b ^ s##c, 7);      \
     } while (0)
 
@@ -44,6 +49,7 @@ __device__ __forceinline__ uint32_t rotr(uint32_t x, int n) { return __funnelshi
 __device__ __forceinline__ void b3_compress_cv(uint32_t cv[8], const uint32_t m[16],
                                                uint64_t counter, uint32_t block_len,
                                                uint32_t flags) {
+    const uint32_t one = kOne;
     uint32_t s0 = cv[0], s1 = cv[1], s2 = cv[2], s3 = cv[3], s4 = cv[4], s5 = cv[5], s6 = cv[6],
              s7 = cv[7];
     uint32_t s8 = kIV[0], s9 = kIV[1], s10 = kIV[2], s11 = kIV[3];

@@ -281,6 +281,38 @@ size_t merkle_scratch_bytes(const Shape &s) {
 
 // Build all parent levels above `n_leaves` leaves stored at tree[0..).
 static int launch_levels(uint32_t *tree, uint64_t n_leaves, int kind, cudaStream_t st,
+                         LaunchLog *log);
+
+bool leaves_range_supported(const Shape &s) { return !(s.hash_kind == 1 && s.log_lanes > 14); }
+
+int launch_leaves_range(const Shape &s, const uint4 *d_cw, uint8_t *d_tree, uint64_t p0,
+                        uint64_t p1, cudaStream_t st) {
+    uint32_t *tree = reinterpret_cast<uint32_t *>(d_tree);
+    const uint64_t n = p1 - p0;
+    const uint4 *cw = d_cw + (p0 << s.log_lanes);
+    uint32_t *leaves = tree + p0 * 8;
+    if (s.hash_kind == 1) {
+        if (s.log_lanes < 6) {
+            b3_leaves_small<<<(unsigned)((n + 255) / 256), 256, 0, st>>>(cw, s.log_lanes, n,
+                                                                      leaves);
+        } else {
+            const int log_c = s.log_lanes - 6;
+            const uint64_t n_chunks = n << log_c;
+            b3_leaves_chunked<<<(unsigned)((n_chunks + 255) / 256), 256, 0, st>>>(
+                cw, s.log_lanes, n_chunks, leaves, log_c);
+        }
+    } else {
+        sha_leaves<<<(unsigned)((n + 127) / 128), 128, 0, st>>>(cw, s.log_lanes, n, leaves);
+    }
+    return 1;
+}
+
+int launch_merkle_levels(const Shape &s, uint8_t *d_tree, cudaStream_t st, LaunchLog *log) {
+    return launch_levels(reinterpret_cast<uint32_t *>(d_tree), s.n_leaves(), s.hash_kind, st,
+                         log);
+}
+
+static int launch_levels(uint32_t *tree, uint64_t n_leaves, int kind, cudaStream_t st,
                          LaunchLog *log) {
     int launches = 0;
     uint64_t in_off = 0, n_in = n_leaves;

@@ -171,6 +171,40 @@ struct T16Lane {
     }
 };
 
+// Same lookups with 8 offset registers: byte positions m and m + 8 differ only
+// in the table half, so off[m + 8] = off[m] ^ (1 << 15).
+struct T16Lane8 {
+    uint32_t off[8];
+    uint32_t s;
+    __device__ __forceinline__ void init() {
+        s = threadIdx.x & 7;
+#pragma unroll
+        for (int m = 0; m < 8; ++m) {
+            const uint32_t k = (m + s) & 15;
+            off[m] = ((k >> 3) << 15) + ((k & 7) << 4);
+        }
+    }
+    __device__ __forceinline__ uint4 rot(uint4 v) const {
+        uint4 r = (s & 4) ? make_uint4(v.y, v.z, v.w, v.x) : v;
+        const uint32_t sh = (s & 3) << 3;
+        return make_uint4(__funnelshift_r(r.x, r.y, sh), __funnelshift_r(r.y, r.z, sh),
+                          __funnelshift_r(r.z, r.w, sh), __funnelshift_r(r.w, r.x, sh));
+    }
+    __device__ __forceinline__ uint4 mul(const char *tb, uint4 v) const {
+        const uint4 vr = rot(v);
+        uint4 acc = make_uint4(0, 0, 0, 0);
+#pragma unroll
+        for (int m = 0; m < 16; ++m) {
+            const uint32_t w = (m < 4) ? vr.x : (m < 8) ? vr.y : (m < 12) ? vr.z : vr.w;
+            const uint32_t x = __byte_perm(w, 0u, 0x4440u | (uint32_t)(m & 3));
+            const uint32_t o = m < 8 ? off[m] : (off[m - 8] ^ 0x8000u);
+            const uint4 e = *reinterpret_cast<const uint4 *>(tb + (x << 7) + o);
+            acc = gf_add(acc, e);
+        }
+        return acc;
+    }
+};
+
 struct TablePassArgs {
     const uint4 *src;   // message (first pass) or codeword
     uint4 *dst;         // codeword
@@ -180,6 +214,7 @@ struct TablePassArgs {
     int log_lanes;
     int src_pos_bits;   // positions are masked to this many bits when reading src
     uint64_t n_tasks;
+    uint64_t task_base; // first task (restricts the pass to a range of positions)
 };
 
 // LAYERS = 2: radix-4 quad (a, b, c, d) at positions B*4Q + g*Q + rr:
@@ -188,8 +223,8 @@ struct TablePassArgs {
 // (the fused 2-layer row op of additive_ntt_f128.rs:829-857, equal to the two
 // single layers applied in order).
 // LAYERS = 1: pair (p, p+H) at layer l with t = twiddle(l, B).
-template <int LAYERS>
-__global__ void __launch_bounds__(512, 1) ntt_table_pass(TablePassArgs a) {
+template <int LAYERS, int THREADS>
+__global__ void __launch_bounds__(THREADS, 1) ntt_table_pass(TablePassArgs a) {
     extern __shared__ uint4 smem[];
     constexpr int NT = LAYERS == 2 ? 3 : 1;
     uint4 *tbl = smem;
@@ -213,7 +248,7 @@ __global__ void __launch_bounds__(512, 1) ntt_table_pass(TablePassArgs a) {
     int64_t cur_b = -1;
 
     for (uint64_t c = c_beg; c < c_end; ++c) {
-        const uint64_t task = c * blockDim.x + threadIdx.x;
+        const uint64_t task = a.task_base + c * blockDim.x + threadIdx.x;
         const uint64_t B = task >> log_task_per_b;  // uniform across the CTA
         if ((int64_t)B != cur_b) {
             __syncthreads();
@@ -268,6 +303,84 @@ __global__ void __launch_bounds__(512, 1) ntt_table_pass(TablePassArgs a) {
     }
 }
 
+// Radix-4 table pass with the next task's four loads issued before the
+// current task's multiplies (register double buffering), so global-memory
+// latency overlaps the shared-memory lookups.
+template <int THREADS>
+__global__ void __launch_bounds__(THREADS, 1) ntt_table_pass2_pf(TablePassArgs a) {
+    extern __shared__ uint4 smem[];
+    uint4 *tbl = smem;
+    uint4 *bases = smem + 3 * kT16Entries;
+    __shared__ uint4 ts[3];
+    __shared__ int tz[3];
+    T16Lane8 lane_ctx;
+    lane_ctx.init();
+    const int log_q = a.ell - a.layer - 2;
+    const int log_task_per_b = log_q + a.log_lanes;
+    const uint64_t lanes_mask = ((uint64_t)1 << a.log_lanes) - 1;
+    const uint64_t q_mask = ((uint64_t)1 << log_q) - 1;
+    const uint64_t src_mask = ((uint64_t)1 << a.src_pos_bits) - 1;
+    const uint64_t chunks = a.n_tasks / blockDim.x;
+    const uint64_t c_beg = chunks * blockIdx.x / gridDim.x;
+    const uint64_t c_end = chunks * (blockIdx.x + 1) / gridDim.x;
+    int64_t cur_b = -1;
+    auto src_index = [&](uint64_t task, int g) -> uint64_t {
+        const uint64_t B = task >> log_task_per_b;
+        const uint64_t rr = (task >> a.log_lanes) & q_mask;
+        const uint64_t p = (B << (log_q + 2)) + ((uint64_t)g << log_q) + rr;
+        return ((p & src_mask) << a.log_lanes) | (task & lanes_mask);
+    };
+    uint4 nxt[4];
+    if (c_beg < c_end) {
+        const uint64_t t0 = a.task_base + c_beg * blockDim.x + threadIdx.x;
+#pragma unroll
+        for (int g = 0; g < 4; ++g) nxt[g] = __ldcs(a.src + src_index(t0, g));
+    }
+    for (uint64_t c = c_beg; c < c_end; ++c) {
+        const uint64_t task = a.task_base + c * blockDim.x + threadIdx.x;
+        const uint64_t B = task >> log_task_per_b;  // uniform across the CTA
+        uint4 v[4];
+#pragma unroll
+        for (int g = 0; g < 4; ++g) v[g] = nxt[g];
+        if (c + 1 < c_end) {
+            const uint64_t tn = task + blockDim.x;
+#pragma unroll
+            for (int g = 0; g < 4; ++g) nxt[g] = __ldcs(a.src + src_index(tn, g));
+        }
+        if ((int64_t)B != cur_b) {
+            __syncthreads();
+            if (threadIdx.x == 0) {
+                ts[0] = a.tw[((uint64_t)1 << a.layer) + B];
+                ts[1] = a.tw[((uint64_t)1 << (a.layer + 1)) + 2 * B];
+                ts[2] = a.tw[((uint64_t)1 << (a.layer + 1)) + 2 * B + 1];
+                for (int i = 0; i < 3; ++i) tz[i] = gf_is_zero(ts[i]);
+            }
+            __syncthreads();
+            t16_build(tbl, bases, ts, 3);
+            cur_b = (int64_t)B;
+        }
+        const char *T0 = reinterpret_cast<const char *>(tbl);
+        const char *T1 = T0 + kT16Entries * 16, *T2 = T1 + kT16Entries * 16;
+        if (!tz[0]) {
+            v[0] = gf_add(v[0], lane_ctx.mul(T0, v[2]));
+            v[1] = gf_add(v[1], lane_ctx.mul(T0, v[3]));
+        }
+        v[2] = gf_add(v[2], v[0]);
+        v[3] = gf_add(v[3], v[1]);
+        if (!tz[1]) v[0] = gf_add(v[0], lane_ctx.mul(T1, v[1]));
+        v[1] = gf_add(v[1], v[0]);
+        if (!tz[2]) v[2] = gf_add(v[2], lane_ctx.mul(T2, v[3]));
+        v[3] = gf_add(v[3], v[2]);
+        const uint64_t rr = (task >> a.log_lanes) & q_mask;
+        const uint64_t ln = task & lanes_mask;
+#pragma unroll
+        for (int g = 0; g < 4; ++g) {
+            const uint64_t p = (B << (log_q + 2)) + ((uint64_t)g << log_q) + rr;
+            __stcs(a.dst + ((p << a.log_lanes) | ln), v[g]);
+        }
+    }
+}
+
 struct DeepArgs {
     const uint4 *src;
     uint4 *dst;
@@ -276,16 +389,48 @@ struct DeepArgs {
     int log_lanes;
     int src_pos_bits;
     uint64_t n_tasks;  // 2^(ell - D) * L
+    uint64_t task_base;
 };
 
+// The narrow layers (depth < D) of one group of 2^D consecutive positions
+// held in registers: layer ell-D+j has 2^j sub-blocks with block index
+// (G << j) | sb (twiddles warp-uniform when the warp shares G).
+template <int D, int P, int MODE>
+__device__ __forceinline__ void narrow_layers(uint4 (&v)[P], const uint4 *tw, int ell,
+                                              uint64_t G) {
+    constexpr int PS = P >> D;  // groups of 2^D inside v (1 for the deep pass)
+#pragma unroll
+    for (int j = 0; j < D; ++j) {
+        const int l = ell - D + j;
+        const int half = (1 << D) >> (j + 1);
+#pragma unroll
+        for (int g = 0; g < PS; ++g) {
+#pragma unroll
+            for (int sb = 0; sb < (1 << j); ++sb) {
+                const uint64_t B = (((G * PS + g)) << j) | (uint64_t)sb;
+                const uint4 t = tw[((uint64_t)1 << l) + B];
+                const bool tz = gf_is_zero(t);
+#pragma unroll
+                for (int i = 0; i < half; ++i) {
+                    uint4 &u = v[g * (1 << D) + sb * 2 * half + i];
+                    uint4 &w = v[g * (1 << D) + sb * 2 * half + i + half];
+                    if (!tz) u = gf_add(u, gf_mul_narrow_m<MODE>(w, t));
+                    w = gf_add(w, u);
+                }
+            }
+        }
+    }
+}
+
 // Last D layers on 2^D consecutive positions per thread (one lane).
-template <int D>
+template <int D, int MODE>
 __global__ void __launch_bounds__(256) ntt_deep_pass(DeepArgs a) {
     constexpr int P = 1 << D;
     const uint64_t lanes_mask = ((uint64_t)1 << a.log_lanes) - 1;
     const uint64_t src_mask = ((uint64_t)1 << a.src_pos_bits) - 1;
-    for (uint64_t task = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; task < a.n_tasks;
-         task += (uint64_t)gridDim.x * blockDim.x) {
+    for (uint64_t it = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; it < a.n_tasks;
+         it += (uint64_t)gridDim.x * blockDim.x) {
+        const uint64_t task = a.task_base + it;
         const uint64_t G = task >> a.log_lanes;
         const uint64_t ln = task & lanes_mask;
         uint4 v[P];
@@ -294,29 +439,89 @@ __global__ void __launch_bounds__(256) ntt_deep_pass(DeepArgs a) {
             const uint64_t pos = (G << D) + i;
             v[i] = __ldcs(a.src + (((pos & src_mask) << a.log_lanes) | ln));
         }
+        narrow_layers<D, P, MODE>(v, a.tw, a.ell, G);
 #pragma unroll
-        for (int j = 0; j < D; ++j) {
-            const int l = a.ell - D + j;
-            constexpr int dummy = 0;
-            (void)dummy;
-            const int half = P >> (j + 1);
+        for (int i = 0; i < P; ++i) {
+            const uint64_t pos = (G << D) + i;
+            __stcs(a.dst + ((pos << a.log_lanes) | ln), v[i]);
+        }
+    }
+}
+
+// Fused tail: the last DT table layers and the DN narrow layers on one group
+// of 2^(DT+DN) consecutive positions per thread (one lane), so the
+// shared-memory lookups of the table layers and the ALU work of the narrow
+// layers overlap inside one pass over the codeword.  Needs >= 512 lanes so
+// every CTA chunk shares the group G (and therefore the tables).
+template <int DT, int DN, int MODE>
+__global__ void __launch_bounds__(512, 1) ntt_tail_pass(DeepArgs a) {
+    extern __shared__ uint4 smem[];
+    constexpr int NT = DT == 2 ? 3 : 1;
+    constexpr int P = 1 << (DT + DN);
+    uint4 *tbl = smem;
+    uint4 *bases = smem + NT * kT16Entries;
+    __shared__ uint4 ts[3];
+    __shared__ int tz[3];
+    T16Lane lane_ctx;
+    lane_ctx.init();
+    const int l0 = a.ell - DT - DN;
+    const uint64_t lanes_mask = ((uint64_t)1 << a.log_lanes) - 1;
+    const uint64_t src_mask = ((uint64_t)1 << a.src_pos_bits) - 1;
+    const uint64_t chunks = a.n_tasks / blockDim.x;
+    const uint64_t c_beg = chunks * blockIdx.x / gridDim.x;
+    const uint64_t c_end = chunks * (blockIdx.x + 1) / gridDim.x;
+    int64_t cur_g = -1;
+    for (uint64_t c = c_beg; c < c_end; ++c) {
+        const uint64_t task = a.task_base + c * blockDim.x + threadIdx.x;
+        const uint64_t G = task >> a.log_lanes;  // uniform across the CTA
+        const uint64_t ln = task & lanes_mask;
+        if ((int64_t)G != cur_g) {
+            __syncthreads();
+            if (threadIdx.x == 0) {
+                ts[0] = a.tw[((uint64_t)1 << l0) + G];
+                if (DT == 2) {
+                    ts[1] = a.tw[((uint64_t)1 << (l0 + 1)) + 2 * G];
+                    ts[2] = a.tw[((uint64_t)1 << (l0 + 1)) + 2 * G + 1];
+                }
+                for (int i = 0; i < NT; ++i) tz[i] = gf_is_zero(ts[i]);
+            }
+            __syncthreads();
+            t16_build(tbl, bases, ts, NT);
+            cur_g = (int64_t)G;
+        }
+        uint4 v[P];
 #pragma unroll
-            for (int sb = 0; sb < (1 << j); ++sb) {
-                const uint64_t B = (G << j) | (uint64_t)sb;
-                const uint4 t = a.tw[((uint64_t)1 << l) + B];
-                const bool tz = gf_is_zero(t);
+        for (int i = 0; i < P; ++i) {
+            const uint64_t pos = (G << (DT + DN)) + i;
+            v[i] = __ldcs(a.src + (((pos & src_mask) << a.log_lanes) | ln));
+        }
+        const char *T0 = reinterpret_cast<const char *>(tbl);
+        // table layer l0: pairs (i, i + P/2)
 #pragma unroll
-                for (int i = 0; i < half; ++i) {
-                    uint4 &u = v[sb * 2 * half + i];
-                    uint4 &w = v[sb * 2 * half + i + half];
-                    if (!tz) u = gf_add(u, gf_mul_narrow(w, t));
+        for (int i = 0; i < P / 2; ++i) {
+            if (!tz[0]) v[i] = gf_add(v[i], lane_ctx.mul(T0, v[i + P / 2]));
+            v[i + P / 2] = gf_add(v[i + P / 2], v[i]);
+        }
+        if (DT == 2) {
+            // table layer l0+1: blocks 2G (first half) and 2G+1 (second half)
+#pragma unroll
+            for (int hb = 0; hb < 2; ++hb) {
+                const char *Tb = T0 + (size_t)(1 + hb) * kT16Entries * 16;
+                const bool z = tz[1 + hb];
+#pragma unroll
+                for (int i = 0; i < P / 4; ++i) {
+                    uint4 &u = v[hb * (P / 2) + i];
+                    uint4 &w = v[hb * (P / 2) + i + P / 4];
+                    if (!z) u = gf_add(u, lane_ctx.mul(Tb, w));
                     w = gf_add(w, u);
                 }
             }
         }
+        // narrow layers: groups of 2^DN positions, group index G * 2^DT + g
+        narrow_layers<DN, P, MODE>(v, a.tw, a.ell, G);
 #pragma unroll
         for (int i = 0; i < P; ++i) {
-            const uint64_t pos = (G << D) + i;
+            const uint64_t pos = (G << (DT + DN)) + i;
             __stcs(a.dst + ((pos << a.log_lanes) | ln), v[i]);
         }
     }
@@ -362,10 +567,10 @@ static inline unsigned grid_for(uint64_t n, int threads, int num_sms, int per_sm
     return (unsigned)g;
 }
 
-static bool table_pass_ok(int ell, int layer, int layers, int log_lanes) {
-    // every CTA chunk (512 tasks) must lie inside one block B
+static bool table_pass_ok(int ell, int layer, int layers, int log_lanes, int log_threads = 9) {
+    // every CTA chunk (blockDim tasks) must lie inside one block B
     const int log_task_per_b = ell - layer - layers + log_lanes;
-    return log_task_per_b >= 9;
+    return log_task_per_b >= log_threads;
 }
 
 static size_t table_smem(int layers) {
@@ -373,11 +578,95 @@ static size_t table_smem(int layers) {
     return (size_t)nt * kT16Entries * 16 + (size_t)nt * 128 * 16;
 }
 
+#define BZ_TAIL_ATTR(DT, DN, M)                                                           \
+    cudaFuncSetAttribute(ntt_tail_pass<DT, DN, M>, cudaFuncAttributeMaxDynamicSharedMemorySize, \
+                         (int)table_smem(DT))
+#define BZ_TAIL_ATTR_M(DT, DN) BZ_TAIL_ATTR(DT, DN, 0); BZ_TAIL_ATTR(DT, DN, 1); BZ_TAIL_ATTR(DT, DN, 2)
+
 void init_ntt_kernels() {
-    cudaFuncSetAttribute(ntt_table_pass<2>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+    cudaFuncSetAttribute(ntt_table_pass<2, 512>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                          (int)table_smem(2));
-    cudaFuncSetAttribute(ntt_table_pass<1>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+    cudaFuncSetAttribute(ntt_table_pass<1, 512>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                          (int)table_smem(1));
+    cudaFuncSetAttribute(ntt_table_pass<2, 256>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                         (int)table_smem(2));
+    cudaFuncSetAttribute(ntt_table_pass2_pf<256>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                         (int)table_smem(2));
+    cudaFuncSetAttribute(ntt_table_pass2_pf<512>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                         (int)table_smem(2));
+    cudaFuncSetAttribute(ntt_table_pass<1, 256>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                         (int)table_smem(1));
+    BZ_TAIL_ATTR_M(1, 1); BZ_TAIL_ATTR_M(1, 2); BZ_TAIL_ATTR_M(1, 3);
+    BZ_TAIL_ATTR_M(2, 1); BZ_TAIL_ATTR_M(2, 2);
+}
+
+template <int D>
+static void launch_deep(const DeepArgs &a, int mode, unsigned grid, cudaStream_t st) {
+    if (mode == 1) ntt_deep_pass<D, 1><<<grid, 256, 0, st>>>(a);
+    else if (mode == 2) ntt_deep_pass<D, 2><<<grid, 256, 0, st>>>(a);
+    else ntt_deep_pass<D, 0><<<grid, 256, 0, st>>>(a);
+}
+
+template <int DT, int DN>
+static void launch_tail(const DeepArgs &a, int mode, unsigned grid, cudaStream_t st) {
+    const size_t sm = table_smem(DT);
+    if (mode == 1) ntt_tail_pass<DT, DN, 1><<<grid, 512, sm, st>>>(a);
+    else if (mode == 2) ntt_tail_pass<DT, DN, 2><<<grid, 512, sm, st>>>(a);
+    else ntt_tail_pass<DT, DN, 0><<<grid, 512, sm, st>>>(a);
+}
+
+int launch_table_pass(const Shape &s, int layer, int layers, const uint4 *src, int src_bits,
+                      uint4 *dst, const uint4 *tw, uint64_t p0, uint64_t p1, int threads,
+                      cudaStream_t st, int num_sms, bool prefetch) {
+    const int ell = s.k_code(), L = s.log_lanes;
+    const int log_q = ell - layer - layers;  // quad / pair stride (positions)
+    TablePassArgs a;
+    a.src = src;
+    a.dst = dst;
+    a.tw = tw;
+    a.ell = ell;
+    a.layer = layer;
+    a.log_lanes = L;
+    a.src_pos_bits = src_bits;
+    // tasks are (B, rr, lane) with B the block index at `layer`
+    const uint64_t b0 = p0 >> (ell - layer), b1 = p1 >> (ell - layer);
+    a.task_base = (b0 << log_q) << L;
+    a.n_tasks = ((b1 - b0) << log_q) << L;
+    const unsigned grid =
+        (unsigned)std::max<uint64_t>(1, std::min<uint64_t>(num_sms, a.n_tasks / threads));
+    if (prefetch && layers == 2) {
+        if (threads == 256) ntt_table_pass2_pf<256><<<grid, 256, table_smem(2), st>>>(a);
+        else ntt_table_pass2_pf<512><<<grid, 512, table_smem(2), st>>>(a);
+    } else if (threads == 256) {
+        if (layers == 2) ntt_table_pass<2, 256><<<grid, 256, table_smem(2), st>>>(a);
+        else ntt_table_pass<1, 256><<<grid, 256, table_smem(1), st>>>(a);
+    } else {
+        if (layers == 2) ntt_table_pass<2, 512><<<grid, 512, table_smem(2), st>>>(a);
+        else ntt_table_pass<1, 512><<<grid, 512, table_smem(1), st>>>(a);
+    }
+    return 1;
+}
+
+int launch_deep_range(const Shape &s, int deep, int mode, const uint4 *src, int src_bits,
+                      uint4 *dst, const uint4 *tw, uint64_t p0, uint64_t p1, cudaStream_t st,
+                      int num_sms) {
+    DeepArgs a;
+    a.src = src;
+    a.dst = dst;
+    a.tw = tw;
+    a.ell = s.k_code();
+    a.log_lanes = s.log_lanes;
+    a.src_pos_bits = src_bits;
+    a.task_base = (p0 >> deep) << s.log_lanes;
+    a.n_tasks = ((p1 - p0) >> deep) << s.log_lanes;
+    const unsigned grid = grid_for(a.n_tasks, 256, num_sms, 8);
+    switch (deep) {
+        case 1: launch_deep<1>(a, mode, grid, st); break;
+        case 2: launch_deep<2>(a, mode, grid, st); break;
+        case 3: launch_deep<3>(a, mode, grid, st); break;
+        default: launch_deep<4>(a, mode, grid, st); break;
+    }
+    return 1;
 }
 
 int launch_ntt(const Shape &s, uint32_t schedule, const uint4 *d_msg, uint4 *d_cw,
@@ -386,6 +675,7 @@ int launch_ntt(const Shape &s, uint32_t schedule, const uint4 *d_msg, uint4 *d_c
         if (log) log->mark(n);
     };
     const int ell = s.k_code(), r = s.log_inv_rate, L = s.log_lanes, b = s.log_dim();
+    const uint64_t P = (uint64_t)1 << ell;
     int launches = 0;
     const uint4 *src = d_msg;
     int src_bits = b;  // message positions are the low b bits of a codeword position
@@ -412,11 +702,21 @@ int launch_ntt(const Shape &s, uint32_t schedule, const uint4 *d_msg, uint4 *d_c
     if (deep > b) deep = b;
     if (deep > 4) deep = 4;
     const bool radix2 = (schedule & SCHED_RADIX2) != 0;
+    const int mode = (int)((schedule >> SCHED_MODE_SHIFT) & 3);
+    const int threads = (schedule & SCHED_SMALL_CTA) ? 256 : 512;
+    const int log_threads = threads == 256 ? 8 : 9;
+    int table_end = ell - deep;
+    // fused tail: the last 1-2 table layers run with the narrow layers
+    int tail_dt = 0;
+    if ((schedule & SCHED_FUSED_TAIL) && deep >= 1 && L >= 9 && table_end > r) {
+        tail_dt = (!radix2 && table_end - r >= 2 && deep <= 2) ? 2 : 1;
+        if (tail_dt + deep > 4) tail_dt = 0;
+        else table_end -= tail_dt;
+    }
     int layer = r;
-    const int table_end = ell - deep;
     while (layer < table_end) {
         const int layers = (!radix2 && layer + 1 < table_end) ? 2 : 1;
-        if (!table_pass_ok(ell, layer, layers, L)) {
+        if (!table_pass_ok(ell, layer, layers, L, log_threads)) {
             // too few tasks per block for table passes: generic single layers
             const uint64_t n_tasks = ((uint64_t)1 << (ell - 1)) << L;
             ntt_generic_layer<<<grid_for(n_tasks, 256, num_sms, 8), 256, 0, st>>>(
@@ -428,44 +728,39 @@ int launch_ntt(const Shape &s, uint32_t schedule, const uint4 *d_msg, uint4 *d_c
             layer += 1;
             continue;
         }
-        TablePassArgs a;
-        a.src = src;
-        a.dst = d_cw;
-        a.tw = d_tw;
-        a.ell = ell;
-        a.layer = layer;
-        a.log_lanes = L;
-        a.src_pos_bits = src_bits;
-        a.n_tasks = ((uint64_t)1 << (ell - layers)) << L;
-        const unsigned grid = (unsigned)std::min<uint64_t>(num_sms, a.n_tasks / 512);
-        if (layers == 2)
-            ntt_table_pass<2><<<grid, 512, table_smem(2), st>>>(a);
-        else
-            ntt_table_pass<1><<<grid, 512, table_smem(1), st>>>(a);
+        launches += launch_table_pass(s, layer, layers, src, src_bits, d_cw, d_tw, 0, P, threads,
+                                      st, num_sms, (schedule & SCHED_PREFETCH) != 0);
         mark(layers == 2 ? (src == d_msg ? "ntt_table_pass2_first" : "ntt_table_pass2")
                          : (src == d_msg ? "ntt_table_pass1_first" : "ntt_table_pass1"));
-        ++launches;
         src = d_cw;
         src_bits = 62;
         layer += layers;
     }
     if (deep > 0) {
-        DeepArgs a;
-        a.src = src;
-        a.dst = d_cw;
-        a.tw = d_tw;
-        a.ell = ell;
-        a.log_lanes = L;
-        a.src_pos_bits = src_bits;
-        a.n_tasks = ((uint64_t)1 << (ell - deep)) << L;
-        const unsigned grid = grid_for(a.n_tasks, 256, num_sms, 8);
-        switch (deep) {
-            case 1: ntt_deep_pass<1><<<grid, 256, 0, st>>>(a); break;
-            case 2: ntt_deep_pass<2><<<grid, 256, 0, st>>>(a); break;
-            case 3: ntt_deep_pass<3><<<grid, 256, 0, st>>>(a); break;
-            default: ntt_deep_pass<4><<<grid, 256, 0, st>>>(a); break;
+        if (tail_dt) {
+            DeepArgs a;
+            a.src = src;
+            a.dst = d_cw;
+            a.tw = d_tw;
+            a.ell = ell;
+            a.log_lanes = L;
+            a.src_pos_bits = src_bits;
+            a.task_base = 0;
+            a.n_tasks = ((uint64_t)1 << (ell - deep - tail_dt)) << L;
+            const unsigned grid = (unsigned)std::min<uint64_t>(num_sms, a.n_tasks / 512);
+            if (tail_dt == 2) {
+                if (deep == 1) launch_tail<2, 1>(a, mode, grid, st);
+                else launch_tail<2, 2>(a, mode, grid, st);
+            } else {
+                if (deep == 1) launch_tail<1, 1>(a, mode, grid, st);
+                else if (deep == 2) launch_tail<1, 2>(a, mode, grid, st);
+                else launch_tail<1, 3>(a, mode, grid, st);
+            }
+            mark("ntt_tail_pass");
+        } else {
+            launch_deep_range(s, deep, mode, src, src_bits, d_cw, d_tw, 0, P, st, num_sms);
+            mark("ntt_deep_pass");
         }
-        mark("ntt_deep_pass");
         ++launches;
     }
     return launches;

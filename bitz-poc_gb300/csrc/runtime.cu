@@ -224,8 +224,7 @@ int enqueue_commit(bz_ctx *ctx, const Shape &s, const uint4 *d_msg, bz_commitmen
         rc = ensure_scratch(ctx, need);
         if (rc) return rc;
     }
-    int n = launch_ntt(s, schedule, d_msg, c->d_cw, d_tw, st, ctx->num_sms);
-    n += launch_merkle(s, c->d_cw, c->d_tree, ctx->scratch, st, ctx->num_sms);
+    int n = launch_commit_kernels(ctx, s, schedule, d_msg, c->d_cw, c->d_tree, d_tw, st, nullptr);
     ctx->launches += (uint64_t)n;
     cudaError_t e = cudaGetLastError();
     if (e != cudaSuccess) return set_err(ctx, BZ_ERR_CUDA, "kernel launch", e);
@@ -233,9 +232,44 @@ int enqueue_commit(bz_ctx *ctx, const Shape &s, const uint4 *d_msg, bz_commitmen
     return BZ_OK;
 }
 
+bz_aux_stream *get_aux(bz_ctx *ctx, cudaStream_t st) {
+    std::lock_guard<std::mutex> g(ctx->aux_mu);
+    auto it = ctx->aux.find(st);
+    if (it != ctx->aux.end()) return &it->second;
+    bz_aux_stream a;
+    if (cudaStreamCreateWithFlags(&a.s, cudaStreamNonBlocking) != cudaSuccess) {
+        cudaGetLastError();
+        return nullptr;
+    }
+    for (auto &e : a.ev) cudaEventCreateWithFlags(&e, cudaEventDisableTiming);
+    return &(ctx->aux[st] = a);
+}
+
+int launch_commit_kernels(bz_ctx *ctx, const Shape &s, uint32_t schedule, const uint4 *d_msg,
+                          uint4 *d_cw, uint8_t *d_tree, const uint4 *d_tw, cudaStream_t st,
+                          LaunchLog *log) {
+    if ((schedule >> SCHED_PIPE_SHIFT) & 3) {
+        bz_aux_stream *ax = get_aux(ctx, st);
+        if (ax) {
+            const int n = launch_commit_pipelined(s, schedule, d_msg, d_cw, d_tree, d_tw, st, ax->s,
+                                                  ax->ev, ctx->num_sms, log);
+            if (n >= 0) return n;
+        }
+    }
+    int n = launch_ntt(s, schedule, d_msg, d_cw, d_tw, st, ctx->num_sms, log);
+    n += launch_merkle(s, d_cw, d_tree, ctx->scratch, st, ctx->num_sms, log);
+    return n;
+}
+
 int fetch_root(bz_commitment *c) {
     bz_ctx *ctx = c->ctx;
     if (c->root_ready) return BZ_OK;
+    if (c->done) {
+        BZ_CUDA(ctx, cudaEventSynchronize(c->done));
+        memcpy(c->root, c->root_slot, 32);
+        c->root_ready = true;
+        return BZ_OK;
+    }
     const uint8_t *src = c->d_tree + (c->shape.tree_nodes() - 1) * 32;
     BZ_CUDA(ctx, cudaMemcpyAsync(ctx->h_small, src, 32, cudaMemcpyDeviceToHost, ctx->stream));
     BZ_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
@@ -287,7 +321,8 @@ int bz_ctx_create(int device, uint64_t mem_budget_bytes, bz_ctx **out) {
     cudaDeviceProp prop;
     cudaGetDeviceProperties(&prop, device);
     ctx->num_sms = prop.multiProcessorCount;
-    if (cudaStreamCreateWithFlags(&ctx->stream, cudaStreamNonBlocking) != cudaSuccess) {
+    if (cudaStreamCreateWithFlags(&ctx->stream, cudaStreamNonBlocking) != cudaSuccess ||
+        cudaStreamCreateWithFlags(&ctx->copy_stream, cudaStreamNonBlocking) != cudaSuccess) {
         delete ctx;
         return BZ_ERR_CUDA;
     }
@@ -326,12 +361,19 @@ int bz_ctx_destroy(bz_ctx *ctx) {
     }
     for (auto *c : live) bz_commitment_free(c);
     for (auto &kv : ctx->twiddles) cudaFree((void *)kv.second);
+    for (auto &kv : ctx->aux) {
+        cudaStreamSynchronize(kv.second.s);
+        for (auto e : kv.second.ev) cudaEventDestroy(e);
+        cudaStreamDestroy(kv.second.s);
+    }
     if (ctx->scratch) cudaFreeAsync(ctx->scratch, ctx->stream);
     cudaStreamSynchronize(ctx->stream);
     cudaFree(ctx->d_small);
     cudaFreeHost(ctx->h_small);
     cudaEventDestroy(ctx->ev0);
     cudaEventDestroy(ctx->ev1);
+    cudaStreamSynchronize(ctx->copy_stream);
+    cudaStreamDestroy(ctx->copy_stream);
     cudaStreamDestroy(ctx->stream);
     delete ctx;
     return BZ_OK;
@@ -450,6 +492,60 @@ int bz_commit(bz_ctx *ctx, const uint64_t *msg, size_t n_words, const bz_params 
     rc = bz_commit_device(ctx, (const uint64_t *)d_msg, n_words, params, out, root);
     dev_free(ctx, d_msg, bytes, true);
     return rc;
+}
+
+int bz_commit_async(bz_ctx *ctx, const uint64_t *msg, size_t n_words, const bz_params *params,
+                    bz_commitment **out) {
+    if (!ctx || !msg || !out) return BZ_ERR_ARG;
+    *out = nullptr;
+    Shape s;
+    std::string why;
+    int rc = shape_from_params(params, s, n_words, why);
+    if (rc) return set_msg(ctx, rc, why);
+    bz_commitment *c = nullptr;
+    rc = alloc_commitment(ctx, s, &c);
+    if (rc) return rc;
+    const size_t bytes = n_words * 16;
+    if (ctx->in_use.load() + bytes > ctx->budget) {
+        bz_commitment_free(c);
+        return set_msg(ctx, BZ_ERR_NOMEM, "memory budget exceeded");
+    }
+    void *d_msg = nullptr;
+    cudaError_t e = cudaMallocAsync(&d_msg, bytes, ctx->copy_stream);
+    if (e != cudaSuccess) {
+        cudaGetLastError();
+        bz_commitment_free(c);
+        return set_err(ctx, BZ_ERR_NOMEM, "message staging", e);
+    }
+    cudaEvent_t copied = nullptr;
+    cudaEventCreateWithFlags(&copied, cudaEventDisableTiming);
+    cudaEventCreateWithFlags(&c->done, cudaEventDisableTiming);
+    e = cudaMemcpyAsync(d_msg, msg, bytes, cudaMemcpyHostToDevice, ctx->copy_stream);
+    if (e == cudaSuccess) e = cudaEventRecord(copied, ctx->copy_stream);
+    if (e == cudaSuccess) e = cudaStreamWaitEvent(ctx->stream, copied, 0);
+    cudaEventDestroy(copied);  // the wait above already captured it
+    if (e != cudaSuccess) {
+        cudaFreeAsync(d_msg, ctx->copy_stream);
+        bz_commitment_free(c);
+        return set_err(ctx, BZ_ERR_CUDA, "H2D message", e);
+    }
+    rc = enqueue_commit(ctx, s, (const uint4 *)d_msg, c, ctx->stream, schedule_for(ctx, s));
+    cudaFreeAsync(d_msg, ctx->stream);
+    if (rc) {
+        bz_commitment_free(c);
+        return rc;
+    }
+    uint8_t *slot = (uint8_t *)ctx->h_small + 32 * (ctx->root_ring++ % 96) + 1024;
+    c->root_slot = slot;
+    cudaMemcpyAsync(slot, c->d_tree + (s.tree_nodes() - 1) * 32, 32, cudaMemcpyDeviceToHost,
+                    ctx->stream);
+    e = cudaEventRecord(c->done, ctx->stream);
+    if (e != cudaSuccess) {
+        bz_commitment_free(c);
+        return set_err(ctx, BZ_ERR_CUDA, "record", e);
+    }
+    *out = c;
+    return BZ_OK;
 }
 
 int bz_commitment_root(bz_commitment *c, uint8_t root[32]) {
@@ -588,6 +684,7 @@ int bz_commitment_free(bz_commitment *c) {
     }
     dev_free(ctx, c->d_cw, c->cw_bytes, true);
     dev_free(ctx, c->d_tree, c->tree_bytes, true);
+    if (c->done) cudaEventDestroy(c->done);
     delete c;
     return BZ_OK;
 }
@@ -614,9 +711,8 @@ int bz_commit_profile(bz_ctx *ctx, const uint64_t *d_msg, size_t n_words,
         LaunchLog log;
         log.st = ctx->stream;
         log.mark("start");
-        int n = launch_ntt(s, schedule_for(ctx, s), (const uint4 *)d_msg, c->d_cw, d_tw,
-                           ctx->stream, ctx->num_sms, &log);
-        n += launch_merkle(s, c->d_cw, c->d_tree, ctx->scratch, ctx->stream, ctx->num_sms, &log);
+        int n = launch_commit_kernels(ctx, s, schedule_for(ctx, s), (const uint4 *)d_msg, c->d_cw,
+                                      c->d_tree, d_tw, ctx->stream, &log);
         ctx->launches += (uint64_t)n;
         cudaError_t e = cudaStreamSynchronize(ctx->stream);
         if (e != cudaSuccess) {

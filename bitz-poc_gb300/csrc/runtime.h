@@ -20,6 +20,15 @@ struct bz_commitment {
     size_t cw_bytes = 0, tree_bytes = 0;
     bool root_ready = false;
     uint8_t root[32] = {0};
+    cudaEvent_t done = nullptr;       // async commits: root copied to root_slot
+    const uint8_t *root_slot = nullptr;
+};
+
+// Auxiliary stream (and its events) paired with a launching stream for the
+// two-stream pipelined commit.
+struct bz_aux_stream {
+    cudaStream_t s = nullptr;
+    cudaEvent_t ev[16] = {};
 };
 
 struct bz_ctx {
@@ -39,6 +48,10 @@ struct bz_ctx {
     void *h_small = nullptr;  // 4 KiB pinned
     void *d_small = nullptr;  // 4 KiB device
     cudaEvent_t ev0 = nullptr, ev1 = nullptr;
+    std::mutex aux_mu;
+    std::map<cudaStream_t, bz_aux_stream> aux;
+    cudaStream_t copy_stream = nullptr;  // host-to-device uploads of async commits
+    uint64_t root_ring = 0;              // next 32-byte slot of h_small for async roots
 };
 
 namespace bz {
@@ -58,4 +71,12 @@ int alloc_commitment(bz_ctx *ctx, const Shape &s, bz_commitment **out);
 int enqueue_commit(bz_ctx *ctx, const Shape &s, const uint4 *d_msg, bz_commitment *c,
                    cudaStream_t st, uint32_t schedule);
 int fetch_root(bz_commitment *c);
+// The auxiliary stream paired with `st` (created on first use; call before a
+// stream capture that will use it).
+bz_aux_stream *get_aux(bz_ctx *ctx, cudaStream_t st);
+// NTT + Merkle kernels of one commit on `st`: the two-stream pipeline when the
+// schedule asks for it and the shape allows it, else the plain sequence.
+int launch_commit_kernels(bz_ctx *ctx, const Shape &s, uint32_t schedule, const uint4 *d_msg,
+                          uint4 *d_cw, uint8_t *d_tree, const uint4 *d_tw, cudaStream_t st,
+                          LaunchLog *log);
 }  // namespace bz

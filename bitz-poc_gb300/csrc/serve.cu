@@ -142,8 +142,8 @@ int start_commit(bz_server *S, Request *r, int slot) {
     const uint4 *d_tw = nullptr;
     int rc = get_twiddles(ctx, s.k_code(), &d_tw);
     if (rc) return rc;
-    int n = launch_ntt(s, schedule_for(ctx, s), r->d_msg, c->d_cw, d_tw, st, ctx->num_sms);
-    n += launch_merkle(s, c->d_cw, c->d_tree, nullptr, st, ctx->num_sms);
+    int n = launch_commit_kernels(ctx, s, schedule_for(ctx, s), r->d_msg, c->d_cw, c->d_tree,
+                                  d_tw, st, nullptr);
     ctx->launches += (uint64_t)n;
     cudaFreeAsync(r->d_msg, st);
     r->d_msg = nullptr;

@@ -101,6 +101,15 @@ int bz_commit_device(bz_ctx *ctx, const uint64_t *d_msg, size_t n_words,
  * through bz_commitment_root.  Used by graph capture and the benchmark. */
 int bz_commit_device_async(bz_ctx *ctx, const uint64_t *d_msg, size_t n_words,
                            const bz_params *params, bz_commitment **out);
+/* Asynchronous bz_commit: the host message is uploaded on the context's copy
+ * stream and the kernels follow on the context stream, so the upload of one
+ * commit overlaps the kernels of the previous one.  Returns without waiting;
+ * `msg` must stay valid (and should be pinned) until bz_commitment_root
+ * returns for this handle.  At most 96 asynchronous commits may be pending
+ * (their roots wait in a ring of pinned slots). */
+int bz_commit_async(bz_ctx *ctx, const uint64_t *msg, size_t n_words, const bz_params *params,
+                    bz_commitment **out);
+/* Root of a commitment (waits for that commitment only). */
 int bz_commitment_root(bz_commitment *c, uint8_t root[32]);
 int bz_commitment_params(const bz_commitment *c, bz_params *params);
 /* Device pointers of the resident codeword (2^(k_code+log_batch_size)

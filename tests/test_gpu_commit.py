@@ -43,8 +43,17 @@ def test_commit_matches_oracle(oracle, ctx, lm, r, lb, kind):
         pd.free()
 
 
-@pytest.mark.parametrize("schedule", [0, 1, 2, 3, 4, 0x10, 0x13, 0x20])
-@pytest.mark.parametrize("lm,r,lb", [(14, 2, 7), (16, 2, 8), (12, 1, 4)])
+SCHEDULES = [0, 1, 2, 3, 4, 0x10, 0x13, 0x20,
+             2 | (1 << 7), 3 | (2 << 7), 0x42, 0x41, 0x43, 0x42 | (1 << 7), 0x42 | (2 << 7),
+             0x52, 0x43 | (1 << 7), 0x44,
+             0x200 | 2, (1 << 10) | 2, (2 << 10) | 0x200 | 2, (3 << 10) | 0x200 | 2,
+             (2 << 10) | 0x200 | 3 | (1 << 7), (1 << 10) | 0x10 | 2, (3 << 10) | 0x200 | 0x11,
+             0x1000 | 2, 0x1200 | 2, 0x1000 | (1 << 10) | 2, 0x1000 | 0]
+
+
+@pytest.mark.parametrize("schedule", SCHEDULES)
+@pytest.mark.parametrize("lm,r,lb", [(14, 2, 7), (12, 1, 4), (18, 2, 9), (20, 2, 10),
+                                     (16, 1, 9), (19, 3, 9)])
 def test_every_schedule_gives_the_same_codeword(oracle, ctx, schedule, lm, r, lb):
     from bitz_gb300 import PcsParams
 
@@ -146,3 +155,30 @@ def test_determinism_and_sensitivity(oracle, ctx):
     assert c1.root == c2.root and c1.root != c3.root
     for d in (d1, d2, d3):
         d.free()
+
+
+def test_async_host_commits_overlap_and_match(oracle, ctx):
+    """bz_commit_async: several commits in flight; each root equals the
+    synchronous commit's."""
+    import ctypes
+
+    from bitz_gb300 import PcsParams, commit
+    from bitz_gb300 import _lib
+
+    L = _lib.lib()
+    p = PcsParams(18 + 7, 2, 9, 1)
+    msgs = [oracle.chacha_words(40 + i, 1 << 18) for i in range(5)]
+    pc = p.to_c()
+    handles = []
+    for m in msgs:
+        h = ctypes.c_void_p()
+        assert L.bz_commit_async(ctx.handle, _lib.ptr(m), m.shape[0], ctypes.byref(pc),
+                                 ctypes.byref(h)) == 0
+        handles.append(h)
+    for m, h in zip(msgs, handles):
+        root = (ctypes.c_uint8 * 32)()
+        assert L.bz_commitment_root(h, root) == 0
+        c, pd = commit(m, p, ctx)
+        assert bytes(root) == c.root
+        pd.free()
+        L.bz_commitment_free(h)
