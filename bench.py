@@ -103,7 +103,7 @@ class _Clocks:
         try:
             self.proc = subprocess.Popen(
                 ["nvidia-smi", f"--id={self.index}", f"--query-gpu={q}", "--format=csv,noheader,nounits",
-                 "-lms", "100"], stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+                 "-lms", "20"], stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
             threading.Thread(target=self._read, daemon=True).start()
         except OSError:
             self.proc = None
@@ -111,6 +111,13 @@ class _Clocks:
     def _read(self):
         for line in self.proc.stdout:
             self.lines.append(line.strip())
+
+    def wait_first(self, timeout_s: float = 5.0):
+        """Block until the sampler produced a line, so samples cover what follows."""
+        t0 = time.perf_counter()
+        while self.proc and not self.lines and time.perf_counter() - t0 < timeout_s:
+            time.sleep(0.01)
+        self.lines.clear()
 
     def stop(self):
         if self.proc:
@@ -232,9 +239,10 @@ def run_gpu(args, ws, rank, local):
     # ---- device-resident timed region -----------------------------------
     launches0 = ctx.kernel_launches()
     clocks = _Clocks(local)
+    clocks.start()
+    clocks.wait_first()
     D.barrier()
     ctx.synchronize()
-    clocks.start()
     step_ms = []
     ctx.timer_begin()
     t_all0 = time.perf_counter()
@@ -585,7 +593,7 @@ def _bench_serve(ctx, bz, args):
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
-    ap.add_argument("--steps", type=int, default=10)
+    ap.add_argument("--steps", type=int, default=50)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--skip-cpu", action="store_true")

@@ -57,6 +57,7 @@ enum : uint32_t {
     SCHED_SMALL_CTA = 0x200,      // 256-thread table passes (room for co-resident CTAs)
     SCHED_PIPE_SHIFT = 10,        // bits 10..11: log2 of the pipeline chunk count
     SCHED_PREFETCH = 0x1000,      // radix-4 table passes double-buffer their loads
+    SCHED_LEAN = 0x2000,          // cap table-pass registers (room for co-resident CTAs)
 };
 uint32_t default_schedule(const Shape &s);
 
@@ -73,7 +74,7 @@ int launch_ntt(const Shape &s, uint32_t schedule, const uint4 *d_msg, uint4 *d_c
 // blocks), used by the pipelined commit.
 int launch_table_pass(const Shape &s, int layer, int layers, const uint4 *src, int src_bits,
                       uint4 *dst, const uint4 *tw, uint64_t p0, uint64_t p1, int threads,
-                      cudaStream_t st, int num_sms, bool prefetch = false);
+                      cudaStream_t st, int num_sms, bool prefetch = false, bool lean = false);
 int launch_deep_range(const Shape &s, int deep, int mode, const uint4 *src, int src_bits,
                       uint4 *dst, const uint4 *tw, uint64_t p0, uint64_t p1, cudaStream_t st,
                       int num_sms);

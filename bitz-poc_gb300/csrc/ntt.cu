@@ -306,8 +306,8 @@ __global__ void __launch_bounds__(THREADS, 1) ntt_table_pass(TablePassArgs a) {
 // Radix-4 table pass with the next task's four loads issued before the
 // current task's multiplies (register double buffering), so global-memory
 // latency overlaps the shared-memory lookups.
-template <int THREADS>
-__global__ void __launch_bounds__(THREADS, 1) ntt_table_pass2_pf(TablePassArgs a) {
+template <int THREADS, int MINB>
+__global__ void __launch_bounds__(THREADS, MINB) ntt_table_pass2_pf(TablePassArgs a) {
     extern __shared__ uint4 smem[];
     uint4 *tbl = smem;
     uint4 *bases = smem + 3 * kT16Entries;
@@ -590,9 +590,11 @@ void init_ntt_kernels() {
                          (int)table_smem(1));
     cudaFuncSetAttribute(ntt_table_pass<2, 256>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                          (int)table_smem(2));
-    cudaFuncSetAttribute(ntt_table_pass2_pf<256>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+    cudaFuncSetAttribute(ntt_table_pass2_pf<256, 1>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                          (int)table_smem(2));
-    cudaFuncSetAttribute(ntt_table_pass2_pf<512>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+    cudaFuncSetAttribute(ntt_table_pass2_pf<256, 2>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                         (int)table_smem(2));
+    cudaFuncSetAttribute(ntt_table_pass2_pf<512, 1>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                          (int)table_smem(2));
     cudaFuncSetAttribute(ntt_table_pass<1, 256>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                          (int)table_smem(1));
@@ -617,7 +619,7 @@ static void launch_tail(const DeepArgs &a, int mode, unsigned grid, cudaStream_t
 
 int launch_table_pass(const Shape &s, int layer, int layers, const uint4 *src, int src_bits,
                       uint4 *dst, const uint4 *tw, uint64_t p0, uint64_t p1, int threads,
-                      cudaStream_t st, int num_sms, bool prefetch) {
+                      cudaStream_t st, int num_sms, bool prefetch, bool lean) {
     const int ell = s.k_code(), L = s.log_lanes;
     const int log_q = ell - layer - layers;  // quad / pair stride (positions)
     TablePassArgs a;
@@ -635,8 +637,12 @@ int launch_table_pass(const Shape &s, int layer, int layers, const uint4 *src, i
     const unsigned grid =
         (unsigned)std::max<uint64_t>(1, std::min<uint64_t>(num_sms, a.n_tasks / threads));
     if (prefetch && layers == 2) {
-        if (threads == 256) ntt_table_pass2_pf<256><<<grid, 256, table_smem(2), st>>>(a);
-        else ntt_table_pass2_pf<512><<<grid, 512, table_smem(2), st>>>(a);
+        if (threads == 256 && lean)
+            ntt_table_pass2_pf<256, 2><<<grid, 256, table_smem(2), st>>>(a);
+        else if (threads == 256)
+            ntt_table_pass2_pf<256, 1><<<grid, 256, table_smem(2), st>>>(a);
+        else
+            ntt_table_pass2_pf<512, 1><<<grid, 512, table_smem(2), st>>>(a);
     } else if (threads == 256) {
         if (layers == 2) ntt_table_pass<2, 256><<<grid, 256, table_smem(2), st>>>(a);
         else ntt_table_pass<1, 256><<<grid, 256, table_smem(1), st>>>(a);
@@ -729,7 +735,8 @@ int launch_ntt(const Shape &s, uint32_t schedule, const uint4 *d_msg, uint4 *d_c
             continue;
         }
         launches += launch_table_pass(s, layer, layers, src, src_bits, d_cw, d_tw, 0, P, threads,
-                                      st, num_sms, (schedule & SCHED_PREFETCH) != 0);
+                                      st, num_sms, (schedule & SCHED_PREFETCH) != 0,
+                                      (schedule & SCHED_LEAN) != 0);
         mark(layers == 2 ? (src == d_msg ? "ntt_table_pass2_first" : "ntt_table_pass2")
                          : (src == d_msg ? "ntt_table_pass1_first" : "ntt_table_pass1"));
         src = d_cw;

@@ -43,16 +43,16 @@ int launch_commit_pipelined(const Shape &s, uint32_t schedule, const uint4 *d_ms
         layer += layers;
     }
     const uint64_t P = (uint64_t)1 << ell;
-    const bool pf = (schedule & SCHED_PREFETCH) != 0;
+    const bool pf = (schedule & SCHED_PREFETCH) != 0, lean = (schedule & SCHED_LEAN) != 0;
     int launches =
-        launch_table_pass(s, r, first, d_msg, b, d_cw, d_tw, 0, P, threads, st, num_sms, pf);
+        launch_table_pass(s, r, first, d_msg, b, d_cw, d_tw, 0, P, threads, st, num_sms, pf, lean);
     if (log) log->mark(first == 2 ? "ntt_table_pass2_first" : "ntt_table_pass1_first");
     for (int k = 0; k < chunks; ++k) {
         const uint64_t p0 = P / chunks * k, p1 = P / chunks * (k + 1);
         for (int layer = r + first; layer < table_end;) {
             const int layers = (!radix2 && layer + 1 < table_end) ? 2 : 1;
             launches += launch_table_pass(s, layer, layers, d_cw, 62, d_cw, d_tw, p0, p1, threads,
-                                          st, num_sms, pf);
+                                          st, num_sms, pf, lean);
             layer += layers;
         }
         cudaEventRecord(ev[k], st);

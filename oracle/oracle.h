@@ -29,6 +29,7 @@ extern "C" {
 #endif
 
 /* ---- GF(2^128), X^128 = X^7 + X^2 + X + 1 ---- */
+const char *orc_clmul_kind(void); /* "pmull" on aarch64+crypto, else "portable" */
 void orc_gf_mul(const uint64_t a[2], const uint64_t b[2], uint64_t out[2]);
 void orc_gf_mul_bitwise(const uint64_t a[2], const uint64_t b[2], uint64_t out[2]);
 void orc_gf_inv(const uint64_t a[2], uint64_t out[2]);

@@ -22,8 +22,11 @@ def build(force: bool = False) -> str:
     src = os.path.join(_HERE, "oracle.c")
     if force or not os.path.exists(_SO) or os.path.getmtime(_SO) < os.path.getmtime(src):
         os.makedirs(os.path.dirname(_SO), exist_ok=True)
+        import platform
+
+        arch = ["-march=armv8-a+crypto"] if platform.machine() in ("aarch64", "arm64") else []
         subprocess.check_call(
-            ["gcc", "-O2", "-fPIC", "-pthread", "-std=c11", "-shared", "-o", _SO, src]
+            ["gcc", "-O2", "-fPIC", "-pthread", "-std=c11", *arch, "-shared", "-o", _SO, src]
         )
     return _SO
 
@@ -44,6 +47,7 @@ _U64 = ctypes.c_uint64
 
 def _declare(L):
     sig = {
+        "orc_clmul_kind": (ctypes.c_char_p, []),
         "orc_gf_mul": (None, [_P, _P, _P]),
         "orc_gf_mul_bitwise": (None, [_P, _P, _P]),
         "orc_gf_inv": (None, [_P, _P]),
@@ -81,6 +85,10 @@ def _declare(L):
 def _p(a: np.ndarray):
     assert a.flags["C_CONTIGUOUS"]
     return a.ctypes.data_as(ctypes.c_void_p)
+
+
+def clmul_kind() -> str:
+    return lib().orc_clmul_kind().decode()
 
 
 def gf(x) -> np.ndarray:
