@@ -12,6 +12,7 @@
 
 #include "bz_internal.h"
 #include "gf128.cuh"
+#include "t16.cuh"
 
 namespace bz {
 
@@ -45,11 +46,30 @@ __device__ void cta_store_pair(gf_wide u0, gf_wide u2, uint64_t *out) {
     }
 }
 
+// Dynamic shared memory of the kernels that multiply by one challenge r
+// through byte tables: the 64 KB table of r and its 128 basis products.
+constexpr size_t kRTableSmem = (size_t)kT16Entries * 16 + 128 * 16;
+
+// Build the byte tables of r in shared memory (all threads; syncs inside).
+__device__ __forceinline__ const char *build_r_table(uint4 *smem, uint4 r) {
+    __shared__ uint4 rs[1];
+    if (threadIdx.x == 0) rs[0] = r;
+    __syncthreads();
+    t16_build(smem, smem + kT16Entries, rs, 1);
+    return reinterpret_cast<const char *>(smem);
+}
+
 // nf[j] = f[2j] + (f[2j] + f[2j+1]) * r (same for b); thread k produces the
-// folded pair (2k, 2k+1) and its message terms.
+// folded pair (2k, 2k+1) and its message terms.  The four multiplies by the
+// challenge r use r's byte tables; the two variable products of the message
+// use the generic carry-less multiply.
 __global__ void __launch_bounds__(256) fold_and_msg_kernel(const uint4 *f, const uint4 *b,
                                                            uint64_t half, uint4 r, uint4 *nf,
                                                            uint4 *nb, uint64_t *partials) {
+    extern __shared__ uint4 smem[];
+    const char *T = build_r_table(smem, r);
+    T16Lane8 lc;
+    lc.init();
     gf_wide u0 = gf_wide_zero(), u2 = gf_wide_zero();
     const uint64_t pairs = half >> 1;
     for (uint64_t k = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; k < pairs;
@@ -57,10 +77,10 @@ __global__ void __launch_bounds__(256) fold_and_msg_kernel(const uint4 *f, const
         const uint4 *fp = f + 4 * k, *bp = b + 4 * k;
         const uint4 f0 = fp[0], f1 = fp[1], f2 = fp[2], f3 = fp[3];
         const uint4 b0 = bp[0], b1 = bp[1], b2 = bp[2], b3 = bp[3];
-        const uint4 x0 = gf_add(f0, gf_mul(gf_add(f0, f1), r));
-        const uint4 x1 = gf_add(f2, gf_mul(gf_add(f2, f3), r));
-        const uint4 y0 = gf_add(b0, gf_mul(gf_add(b0, b1), r));
-        const uint4 y1 = gf_add(b2, gf_mul(gf_add(b2, b3), r));
+        const uint4 x0 = gf_add(f0, lc.mul(T, gf_add(f0, f1)));
+        const uint4 x1 = gf_add(f2, lc.mul(T, gf_add(f2, f3)));
+        const uint4 y0 = gf_add(b0, lc.mul(T, gf_add(b0, b1)));
+        const uint4 y1 = gf_add(b2, lc.mul(T, gf_add(b2, b3)));
         nf[2 * k] = x0;
         nf[2 * k + 1] = x1;
         nb[2 * k] = y0;
@@ -125,7 +145,8 @@ int launch_fold_and_msg(const uint4 *d_f, const uint4 *d_b, size_t n, uint4 r, u
                         int num_sms) {
     const uint64_t half = n / 2;
     const int grid = std::min(msg_grid(half / 2, num_sms), 1024);
-    fold_and_msg_kernel<<<grid, 256, 0, st>>>(d_f, d_b, half, r, d_nf, d_nb, d_partials);
+    fold_and_msg_kernel<<<grid, 256, kRTableSmem, st>>>(d_f, d_b, half, r, d_nf, d_nb,
+                                                         d_partials);
     finish_msg_kernel<<<1, 32, 0, st>>>(d_partials, grid, d_msg_out);
     return 2;
 }
@@ -141,19 +162,24 @@ int launch_round_msg(const uint4 *d_f, const uint4 *d_b, size_t n, uint64_t *d_p
 
 // One partial_eval_lsb round: out[i] = in[2i] + (in[2i] + in[2i+1]) * r
 // (= in[2i]*(1+r) + in[2i+1]*r exactly, ligerito.rs:1686-1691).
-__global__ void partial_eval_round_kernel(const uint4 *in, uint64_t half, uint4 r, uint4 *out) {
+__global__ void __launch_bounds__(256) partial_eval_round_kernel(const uint4 *in, uint64_t half,
+                                                                 uint4 r, uint4 *out) {
+    extern __shared__ uint4 smem[];
+    const char *T = build_r_table(smem, r);
+    T16Lane8 lc;
+    lc.init();
     for (uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; i < half;
          i += (uint64_t)gridDim.x * blockDim.x) {
         const uint4 v0 = in[2 * i], v1 = in[2 * i + 1];
-        out[i] = gf_add(v0, gf_mul(gf_add(v0, v1), r));
+        out[i] = gf_add(v0, lc.mul(T, gf_add(v0, v1)));
     }
 }
 
 int launch_partial_eval_round(const uint4 *d_in, size_t n, uint4 r, uint4 *d_out,
                               cudaStream_t st) {
     const uint64_t half = n / 2;
-    const unsigned grid = (unsigned)std::min<uint64_t>((half + 255) / 256, 8192);
-    partial_eval_round_kernel<<<std::max(grid, 1u), 256, 0, st>>>(d_in, half, r, d_out);
+    const unsigned grid = (unsigned)std::min<uint64_t>((half + 255) / 256, 152 * 3);
+    partial_eval_round_kernel<<<std::max(grid, 1u), 256, kRTableSmem, st>>>(d_in, half, r, d_out);
     return 1;
 }
 
@@ -267,6 +293,10 @@ __global__ void __launch_bounds__(256) phi_kernel(const uint4 *eq_hi, uint64_t n
 
 void init_fold_kernels() {
     cudaFuncSetAttribute(phi_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, 65536);
+    cudaFuncSetAttribute(fold_and_msg_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                         (int)kRTableSmem);
+    cudaFuncSetAttribute(partial_eval_round_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                         (int)kRTableSmem);
 }
 
 int launch_phi(const uint4 *d_eq_hi, size_t n, const uint4 *d_eq_r2, uint4 *d_out,

@@ -69,6 +69,10 @@ extern "C" int bz_fold_and_msg_lsb_static(const uint64_t *d_f, const uint64_t *d
                 cudaGetLastError();
                 return BZ_ERR_CUDA;
             }
+            // the fold kernel keeps the challenge's byte tables in 66 KB of
+            // dynamic shared memory; opt in for this device (no allocation)
+            bz::init_fold_kernels();
+            if (cudaGetLastError() != cudaSuccess) return BZ_ERR_CUDA;
             g_partials_addr[dev] = (uint64_t *)p;
             g_num_sms[dev] = sms;
         }

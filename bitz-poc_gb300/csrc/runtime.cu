@@ -394,15 +394,17 @@ int bz_ctx_memory(const bz_ctx *ctx, uint64_t *in_use, uint64_t *budget) {
     return BZ_OK;
 }
 
+// Stream-ordered on the context stream (the context's memory pool): the
+// memory is valid for work enqueued on that stream after the allocation and
+// is recycled once the work enqueued before the free has finished.
 int bz_device_alloc(bz_ctx *ctx, size_t bytes, void **dptr) {
     if (!ctx || !dptr) return BZ_ERR_ARG;
-    BZ_CUDA(ctx, cudaMalloc(dptr, bytes ? bytes : 16));
+    BZ_CUDA(ctx, cudaMallocAsync(dptr, bytes ? bytes : 16, ctx->stream));
     return BZ_OK;
 }
 int bz_device_free(bz_ctx *ctx, void *dptr) {
     if (!ctx) return BZ_ERR_ARG;
-    BZ_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
-    BZ_CUDA(ctx, cudaFree(dptr));
+    if (dptr) BZ_CUDA(ctx, cudaFreeAsync(dptr, ctx->stream));
     return BZ_OK;
 }
 int bz_memcpy_h2d(bz_ctx *ctx, void *dst, const void *src, size_t bytes) {

@@ -163,7 +163,28 @@ def make_roots():
         json.dump({"inputs": "ChaCha20 words of the given seed", "roots": res}, fh, indent=1)
 
 
+def add_root(lm, r, lb, kind, seed):
+    """Compute one more oracle root and merge it into roots.json."""
+    from oracle import oracle as O
+
+    path = os.path.join(HERE, "roots.json")
+    with open(path) as fh:
+        data = json.load(fh)
+    msg = O.chacha_words(seed, 1 << lm)
+    _, _, root = O.commit(msg, r, lb, kind, n_threads=os.cpu_count() or 1)
+    entry = {"log_msg_len": lm, "log_inv_rate": r, "log_batch_size": lb,
+             "hash": "blake3" if kind else "sha256", "seed": seed, "root": root.hex()}
+    data["roots"] = [e for e in data["roots"] if (e["log_msg_len"], e["seed"], e["hash"]) !=
+                     (lm, seed, entry["hash"])] + [entry]
+    with open(path, "w") as fh:
+        json.dump(data, fh, indent=1)
+    print(entry)
+
+
 if __name__ == "__main__":
+    if sys.argv[1:2] == ["root"]:
+        add_root(*[int(x) for x in sys.argv[2:7]])
+        sys.exit(0)
     which = sys.argv[1:] or ["ghash", "chacha", "cmt1", "roots"]
     if "ghash" in which:
         make_ghash()
