@@ -21,3 +21,5 @@ from .pcs import (  # noqa: F401
     default_context,
     ligero_commit,
 )
+from .transcript import Blake3Transcript, ZincChallenger, blake3_xof, pow_first_nonce  # noqa: F401,E402
+from .opening import L0Config, L0Opening, open_l0  # noqa: F401,E402

@@ -77,6 +77,26 @@ _SIGS = {
     "bz_phi_from_words": (_I, [_P, _P, _S, _P, _P]),
     "bz_chacha_fill_device": (_I, [_P, _U64, _U64, _P, _S]),
     "bz_chacha_fill_host": (_I, [_U64, _U64, _P, _S, _I]),
+    "bz_transcript_create": (_I, [_PP]),
+    "bz_transcript_clone": (_I, [_P, _PP]),
+    "bz_transcript_destroy": (_I, [_P]),
+    "bz_transcript_absorb": (_I, [_P, _P, _S]),
+    "bz_transcript_absorb_slice": (_I, [_P, _P, _S]),
+    "bz_transcript_challenge": (_I, [_P, _P, _S]),
+    "bz_transcript_sample_f128": (_I, [_P, _P]),
+    "bz_transcript_observe_f128": (_I, [_P, _P]),
+    "bz_transcript_fill_sampling_bytes": (_I, [_P, _P, _S]),
+    "bz_transcript_state_digest": (_I, [_P, _P]),
+    "bz_blake3_xof": (_I, [_P, _S, _P, _S]),
+    "bz_pow_first_nonce": (_I, [_P, _P, _S, _U32, _U64, _U64, ctypes.POINTER(_U64)]),
+    "bz_transcript_grind_pow": (_I, [_P, _P, _U32, ctypes.POINTER(_U64)]),
+    "bz_transcript_verify_pow": (_I, [_P, _U64, _U32, ctypes.POINTER(_I)]),
+    "bz_ligerito_open_l0": (_I, [_P, _P, _P, _P, _P, _P, _P, _PP]),
+    "bz_l0_opening_sizes": (_I, [_P, _P]),
+    "bz_l0_opening_copy": (_I, [_P, _P, _P, _P, _P, _P, _P, _P, _P, _P]),
+    "bz_l0_opening_level1": (_P, [_P]),
+    "bz_l0_opening_folded": (_I, [_P, _PP, _PP, ctypes.POINTER(_S)]),
+    "bz_l0_opening_free": (_I, [_P]),
     "bz_autotune": (_I, [_P, ctypes.POINTER(Params), _I, ctypes.POINTER(_U32)]),
     "bz_schedule_get": (_I, [_P, ctypes.POINTER(Params), ctypes.POINTER(_U32)]),
     "bz_schedule_set": (_I, [_P, ctypes.POINTER(Params), _U32]),

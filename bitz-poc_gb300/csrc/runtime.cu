@@ -69,12 +69,6 @@ void hgf_inv(const uint64_t a[2], uint64_t out[2]) {
 // ===========================================================================
 // Context helpers.
 // ===========================================================================
-#define BZ_CUDA(ctx, call)                                                      \
-    do {                                                                        \
-        cudaError_t e_ = (call);                                                \
-        if (e_ != cudaSuccess) return bz::set_err((ctx), BZ_ERR_CUDA, #call, e_); \
-    } while (0)
-
 namespace bz {
 
 int set_err(bz_ctx *ctx, int code, const char *what, cudaError_t e) {

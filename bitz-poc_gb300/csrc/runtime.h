@@ -54,6 +54,13 @@ struct bz_ctx {
     uint64_t root_ring = 0;              // next 32-byte slot of h_small for async roots
 };
 
+// Return BZ_ERR_CUDA (recording the failing call) when a CUDA call fails.
+#define BZ_CUDA(ctx, call)                                                      \
+    do {                                                                        \
+        cudaError_t e_ = (call);                                                \
+        if (e_ != cudaSuccess) return bz::set_err((ctx), BZ_ERR_CUDA, #call, e_); \
+    } while (0)
+
 namespace bz {
 inline uint64_t shape_key(const Shape &s) {
     return (uint64_t)s.log_msg_len | ((uint64_t)s.log_inv_rate << 8) |

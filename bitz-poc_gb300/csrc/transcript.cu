@@ -1,0 +1,307 @@
+// Fiat-Shamir transcript of the opening, on the host.
+//
+// The state is an incremental BLAKE3 hasher (the `blake3` crate's Hasher that
+// BitZ's Blake3Transcript wraps, src/transcript/mod.rs:18-96); squeezes read
+// its extended output (finalize_xof) without consuming the state.  Everything
+// absorbed here is a few bytes per protocol message, so the hasher is plain
+// portable C++; the bulk hashing of the commitment stays on the GPU.
+//
+// The incremental hasher keeps the chunk being filled and a stack of the
+// chaining values of completed subtrees (one per set bit of the number of
+// completed chunks): completing chunk c pushes its CV and merges the top of
+// the stack once for every trailing zero bit of c + 1, which builds exactly
+// the left-complete binary tree of the BLAKE3 specification.  A completed
+// chunk is only pushed when more input arrives, so the last chunk (and with
+// it the root node) is always still open at finalisation.
+#include <string.h>
+
+#include <new>
+
+#include "../../include/bitz_gpu.h"
+#include "transcript.h"
+
+namespace bzh {
+
+namespace {
+
+constexpr uint32_t kIV[8] = {0x6A09E667u, 0xBB67AE85u, 0x3C6EF372u, 0xA54FF53Au,
+                             0x510E527Fu, 0x9B05688Cu, 0x1F83D9ABu, 0x5BE0CD19u};
+// Message word order of round i+1 is the order of round i taken through this
+// permutation (BLAKE3 specification, section 2.2).
+constexpr uint8_t kPerm[16] = {2, 6, 3, 10, 7, 0, 4, 13, 1, 11, 12, 5, 9, 14, 15, 8};
+constexpr uint32_t CHUNK_START = 1, CHUNK_END = 2, PARENT = 4, ROOT = 8;
+
+inline uint32_t rotr(uint32_t x, int n) { return (x >> n) | (x << (32 - n)); }
+
+inline void mix(uint32_t s[16], int a, int b, int c, int d, uint32_t x, uint32_t y) {
+    s[a] = s[a] + s[b] + x;
+    s[d] = rotr(s[d] ^ s[a], 16);
+    s[c] = s[c] + s[d];
+    s[b] = rotr(s[b] ^ s[c], 12);
+    s[a] = s[a] + s[b] + y;
+    s[d] = rotr(s[d] ^ s[a], 8);
+    s[c] = s[c] + s[d];
+    s[b] = rotr(s[b] ^ s[c], 7);
+}
+
+// Full 16-word compression output: out[i] = s[i] ^ s[i+8] and
+// out[i+8] = s[i+8] ^ cv[i].
+void compress(const uint32_t cv[8], const uint32_t block[16], uint64_t counter,
+              uint32_t block_len, uint32_t flags, uint32_t out[16]) {
+    uint32_t s[16] = {cv[0], cv[1], cv[2], cv[3], cv[4], cv[5], cv[6], cv[7],
+                      kIV[0], kIV[1], kIV[2], kIV[3], (uint32_t)counter,
+                      (uint32_t)(counter >> 32), block_len, flags};
+    uint32_t m[16], t[16];
+    memcpy(m, block, sizeof m);
+    for (int r = 0; r < 7; ++r) {
+        mix(s, 0, 4, 8, 12, m[0], m[1]);
+        mix(s, 1, 5, 9, 13, m[2], m[3]);
+        mix(s, 2, 6, 10, 14, m[4], m[5]);
+        mix(s, 3, 7, 11, 15, m[6], m[7]);
+        mix(s, 0, 5, 10, 15, m[8], m[9]);
+        mix(s, 1, 6, 11, 12, m[10], m[11]);
+        mix(s, 2, 7, 8, 13, m[12], m[13]);
+        mix(s, 3, 4, 9, 14, m[14], m[15]);
+        for (int i = 0; i < 16; ++i) t[i] = m[kPerm[i]];
+        memcpy(m, t, sizeof m);
+    }
+    for (int i = 0; i < 8; ++i) {
+        out[i] = s[i] ^ s[i + 8];
+        out[i + 8] = s[i + 8] ^ cv[i];
+    }
+}
+
+void load_words(const uint8_t *p, size_t len, uint32_t w[16]) {
+    uint8_t b[64] = {0};
+    memcpy(b, p, len);
+    for (int i = 0; i < 16; ++i)
+        w[i] = (uint32_t)b[4 * i] | ((uint32_t)b[4 * i + 1] << 8) |
+               ((uint32_t)b[4 * i + 2] << 16) | ((uint32_t)b[4 * i + 3] << 24);
+}
+
+}  // namespace
+
+void Node::chaining_value(uint32_t out[8]) const {
+    uint32_t o[16];
+    compress(cv, block, counter, block_len, flags, o);
+    memcpy(out, o, 32);
+}
+
+void Node::root_output(uint8_t *out, size_t n) const {
+    for (uint64_t t = 0; 64 * t < n; ++t) {
+        uint32_t o[16];
+        compress(cv, block, t, block_len, flags | ROOT, o);
+        for (size_t i = 0; i < 64 && 64 * t + i < n; ++i)
+            out[64 * t + i] = (uint8_t)(o[i / 4] >> (8 * (i % 4)));
+    }
+}
+
+Hasher::Hasher() { reset_chunk(0); }
+
+void Hasher::reset_chunk(uint64_t index) {
+    memcpy(chunk_cv_, kIV, sizeof chunk_cv_);
+    chunk_index_ = index;
+    buf_len_ = 0;
+    blocks_done_ = 0;
+}
+
+void Hasher::push_chunk_cv(const uint32_t cv[8], uint64_t completed) {
+    uint32_t cur[8];
+    memcpy(cur, cv, sizeof cur);
+    for (; (completed & 1) == 0; completed >>= 1) {
+        Node p;
+        memcpy(p.cv, kIV, sizeof p.cv);
+        memcpy(p.block, stack_[--depth_], 32);
+        memcpy(p.block + 8, cur, 32);
+        p.counter = 0;
+        p.block_len = 64;
+        p.flags = PARENT;
+        p.chaining_value(cur);
+    }
+    memcpy(stack_[depth_++], cur, 32);
+}
+
+void Hasher::update(const uint8_t *p, size_t n) {
+    while (n) {
+        if (buf_len_ == 64) {
+            // a full block with more input behind it is never the chunk's last
+            if (blocks_done_ == 15) {
+                Node last = chunk_node();
+                uint32_t cv[8];
+                last.chaining_value(cv);
+                push_chunk_cv(cv, chunk_index_ + 1);
+                reset_chunk(chunk_index_ + 1);
+            } else {
+                uint32_t w[16], o[16];
+                load_words(buf_, 64, w);
+                compress(chunk_cv_, w, chunk_index_, 64, blocks_done_ == 0 ? CHUNK_START : 0, o);
+                memcpy(chunk_cv_, o, 32);
+                ++blocks_done_;
+                buf_len_ = 0;
+            }
+        }
+        size_t take = 64 - buf_len_;
+        if (take > n) take = n;
+        memcpy(buf_ + buf_len_, p, take);
+        buf_len_ += (uint32_t)take;
+        p += take;
+        n -= take;
+    }
+}
+
+Node Hasher::chunk_node() const {
+    Node c;
+    memcpy(c.cv, chunk_cv_, sizeof c.cv);
+    load_words(buf_, buf_len_, c.block);
+    c.counter = chunk_index_;
+    c.block_len = buf_len_;
+    c.flags = (blocks_done_ == 0 ? CHUNK_START : 0) | CHUNK_END;
+    return c;
+}
+
+Node Hasher::root_node() const {
+    Node n = chunk_node();
+    for (int i = depth_ - 1; i >= 0; --i) {
+        uint32_t right[8];
+        n.chaining_value(right);
+        Node p;
+        memcpy(p.cv, kIV, sizeof p.cv);
+        memcpy(p.block, stack_[i], 32);
+        memcpy(p.block + 8, right, 32);
+        p.counter = 0;
+        p.block_len = 64;
+        p.flags = PARENT;
+        n = p;
+    }
+    return n;
+}
+
+void Hasher::xof(uint8_t *out, size_t n) const { root_node().root_output(out, n); }
+
+// ---- Blake3Transcript (src/transcript/mod.rs:18-96, traits.rs:371-376) ----
+
+void Transcript::absorb_slice(const uint8_t *p, size_t n) {
+    uint8_t hdr[9];
+    hdr[0] = 0x06;
+    for (int i = 0; i < 8; ++i) hdr[1 + i] = (uint8_t)((uint64_t)n >> (8 * i));
+    h.update(hdr, 9);
+    h.update(p, n);
+    const uint8_t tail = 0x07;
+    h.update(&tail, 1);
+}
+
+void Transcript::challenge(uint8_t *out, size_t n) {
+    h.xof(out, n);
+    const uint8_t open = 0x12, close = 0x34;
+    h.update(&open, 1);
+    h.update(out, n);
+    h.update(&close, 1);
+}
+
+void Transcript::sample_f128(uint64_t out[2]) {
+    uint8_t b[16];
+    challenge(b, 16);
+    out[0] = out[1] = 0;
+    for (int i = 0; i < 8; ++i) {
+        out[0] |= (uint64_t)b[i] << (8 * i);
+        out[1] |= (uint64_t)b[8 + i] << (8 * i);
+    }
+}
+
+void Transcript::observe_f128(const uint64_t v[2]) {
+    uint8_t b[16];
+    for (int i = 0; i < 8; ++i) {
+        b[i] = (uint8_t)(v[0] >> (8 * i));
+        b[8 + i] = (uint8_t)(v[1] >> (8 * i));
+    }
+    absorb_slice(b, 16);
+}
+
+void Transcript::fill_sampling_bytes(uint8_t *out, size_t n) {
+    static const char kTag[] = "bitz/sampling-read/v1";
+    h.xof(out, n);
+    h.update((const uint8_t *)kTag, sizeof kTag - 1);
+    uint8_t len[8];
+    for (int i = 0; i < 8; ++i) len[i] = (uint8_t)((uint64_t)n >> (8 * i));
+    h.update(len, 8);
+    h.update(out, n);
+}
+
+}  // namespace bzh
+
+struct bz_transcript {
+    bzh::Transcript t;
+};
+
+extern "C" {
+
+int bz_transcript_create(bz_transcript **out) {
+    if (!out) return BZ_ERR_ARG;
+    *out = new (std::nothrow) bz_transcript();
+    return *out ? BZ_OK : BZ_ERR_NOMEM;
+}
+
+int bz_transcript_clone(const bz_transcript *t, bz_transcript **out) {
+    if (!t || !out) return BZ_ERR_ARG;
+    *out = new (std::nothrow) bz_transcript(*t);
+    return *out ? BZ_OK : BZ_ERR_NOMEM;
+}
+
+int bz_transcript_destroy(bz_transcript *t) {
+    delete t;
+    return BZ_OK;
+}
+
+int bz_transcript_absorb(bz_transcript *t, const uint8_t *data, size_t len) {
+    if (!t || (len && !data)) return BZ_ERR_ARG;
+    t->t.h.update(data, len);
+    return BZ_OK;
+}
+
+int bz_transcript_absorb_slice(bz_transcript *t, const uint8_t *data, size_t len) {
+    if (!t || (len && !data)) return BZ_ERR_ARG;
+    t->t.absorb_slice(data, len);
+    return BZ_OK;
+}
+
+int bz_transcript_challenge(bz_transcript *t, uint8_t *out, size_t len) {
+    if (!t || (len && !out)) return BZ_ERR_ARG;
+    t->t.challenge(out, len);
+    return BZ_OK;
+}
+
+int bz_transcript_sample_f128(bz_transcript *t, uint64_t out[2]) {
+    if (!t || !out) return BZ_ERR_ARG;
+    t->t.sample_f128(out);
+    return BZ_OK;
+}
+
+int bz_transcript_observe_f128(bz_transcript *t, const uint64_t v[2]) {
+    if (!t || !v) return BZ_ERR_ARG;
+    t->t.observe_f128(v);
+    return BZ_OK;
+}
+
+int bz_transcript_fill_sampling_bytes(bz_transcript *t, uint8_t *out, size_t len) {
+    if (!t || (len && !out)) return BZ_ERR_ARG;
+    t->t.fill_sampling_bytes(out, len);
+    return BZ_OK;
+}
+
+int bz_transcript_state_digest(const bz_transcript *t, uint8_t out[32]) {
+    if (!t || !out) return BZ_ERR_ARG;
+    t->t.h.xof(out, 32);
+    return BZ_OK;
+}
+
+int bz_blake3_xof(const uint8_t *data, size_t len, uint8_t *out, size_t out_len) {
+    if ((len && !data) || (out_len && !out)) return BZ_ERR_ARG;
+    bzh::Hasher h;
+    h.update(data, len);
+    h.xof(out, out_len);
+    return BZ_OK;
+}
+
+}  // extern "C"
+
+bzh::Transcript *bz_transcript_inner(bz_transcript *t) { return t ? &t->t : nullptr; }

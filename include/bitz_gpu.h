@@ -32,7 +32,7 @@ typedef enum {
     BZ_ERR_BUSY = 5,     /* server queue full */
     BZ_ERR_TIMEOUT = 6,  /* a bounded wait ran out */
     BZ_ERR_STATE = 7,    /* handle in the wrong state (e.g. opened twice, freed) */
-    BZ_ERR_NOTFOUND = 8  /* unknown request id */
+    BZ_ERR_NOTFOUND = 8  /* unknown request id; no proof-of-work nonce in the range */
 } bz_status;
 
 /* Merkle hash (flock-core/src/hash.rs:21-27; merkle.rs:203-232). */
@@ -263,6 +263,104 @@ int bz_sv_fold(bz_ctx *ctx, const uint64_t *d_packed, const uint64_t *d_eq, size
  * 128 elements. */
 int bz_phi_from_words(bz_ctx *ctx, const uint64_t *d_eq_hi, size_t n, const uint64_t *eq_r2,
                       uint64_t *d_out);
+
+/* ---- Fiat-Shamir transcript (host) ----------------------------------------- */
+/* BitZ's Blake3Transcript (src/transcript/mod.rs:18-96): an incremental
+ * BLAKE3 hasher over everything absorbed; squeezes read its extended output
+ * without consuming the state.  Host-only and cheap; not thread-safe per
+ * handle. */
+typedef struct bz_transcript bz_transcript;
+int bz_transcript_create(bz_transcript **out);
+int bz_transcript_clone(const bz_transcript *t, bz_transcript **out);
+int bz_transcript_destroy(bz_transcript *t);
+/* absorb_inner (mod.rs:81-95): a plain hasher update. */
+int bz_transcript_absorb(bz_transcript *t, const uint8_t *data, size_t len);
+/* absorb_slice (src/transcript/traits.rs:371-376): 0x06 || len u64 LE ||
+ * data || 0x07.  Every ZincChallenger observation (src/ligerito_flock.rs:
+ * 36-62) is one absorb_slice. */
+int bz_transcript_absorb_slice(bz_transcript *t, const uint8_t *data, size_t len);
+/* get_challenge of a len-byte type without padding bits (mod.rs:65-80):
+ * squeeze len bytes, then absorb 0x12 || bytes || 0x34. */
+int bz_transcript_challenge(bz_transcript *t, uint8_t *out, size_t len);
+/* get_field_challenge::<Gf128> = ZincChallenger::sample_f128 (:64-67). */
+int bz_transcript_sample_f128(bz_transcript *t, uint64_t out[2]);
+/* ZincChallenger::observe_f128 (:41-46): absorb_slice of lo LE || hi LE. */
+int bz_transcript_observe_f128(bz_transcript *t, const uint64_t v[2]);
+/* fill_sampling_bytes (mod.rs:58-63). */
+int bz_transcript_fill_sampling_bytes(bz_transcript *t, uint8_t *out, size_t len);
+/* state_digest (mod.rs:40-42). */
+int bz_transcript_state_digest(const bz_transcript *t, uint8_t out[32]);
+/* BLAKE3 extended output of one message (the `blake3` crate's
+ * finalize_xof().fill), on the host. */
+int bz_blake3_xof(const uint8_t *data, size_t len, uint8_t *out, size_t out_len);
+
+/* ---- proof of work (GPU) ---------------------------------------------------- */
+/* first_pow_nonce (src/utils/blake3x4.rs:42-69; the parallel
+ * smallest_pow_nonce :71-120 returns the same nonce): the smallest nonce in
+ * [start, end) such that blake3(prefix || nonce u64 LE) has >= bits leading
+ * zero bits (most significant bit of byte 0 first).  prefix_len + 8 <= 64;
+ * bits <= 256; bits == 0 gives start.  BZ_ERR_NOTFOUND when no nonce in the
+ * range passes.  Synchronous (launches on the context stream). */
+int bz_pow_first_nonce(bz_ctx *ctx, const uint8_t *prefix, size_t prefix_len, uint32_t bits,
+                       uint64_t start, uint64_t end, uint64_t *nonce);
+/* ZincChallenger::grind_pow (src/ligerito_flock.rs:70-99): seed = one
+ * sample_f128 as 16 LE bytes; nonce = 0 when bits == 0, else the smallest
+ * passing nonce of blake3(seed || nonce) (searched on the GPU); then
+ * absorb_slice(nonce LE). */
+int bz_transcript_grind_pow(bz_ctx *ctx, bz_transcript *t, uint32_t bits, uint64_t *nonce);
+/* ZincChallenger::verify_pow (:101-113), on the host; *ok = 0 or 1. */
+int bz_transcript_verify_pow(bz_transcript *t, uint64_t nonce, uint32_t bits, int *ok);
+
+/* ---- level-0 Ligerito opening ---------------------------------------------- */
+/* The level-0 part of recursive_prover_with_basis_initial_impl
+ * (flock-core/src/pcs/ligerito.rs:3566-3720; entered from
+ * recursive_prover_with_basis, :3455-3487, by BinaryPcs::open_basis,
+ * src/binary_pcs.rs:341-367) against a device-resident commitment: the
+ * transcript prefix, the initial_k lane folds (with fold grinding), the
+ * level-1 ligero_commit of the folded witness, the query grind, the sampled
+ * queries and alpha_0, and the opened rows with their Merkle multi-proof.
+ * Requires initial_k == the commitment's log_batch_size and no level-1 OOD
+ * samples (ood_samples[1] == 0). */
+typedef struct {
+    uint32_t initial_k;           /* ProverConfig::initial_k */
+    uint32_t recursive_k0;        /* recursive_ks[0] */
+    uint32_t log_inv_rate1;       /* log_inv_rates[1] */
+    uint32_t fold_grinding_bits0; /* fold_grinding_bits[0] */
+    uint32_t grinding_bits0;      /* grinding_bits[0] */
+    uint32_t queries0;            /* queries[0] */
+    uint32_t hash_kind;           /* merkle_hash of the level-1 commitment */
+} bz_l0_config;
+typedef struct {
+    size_t n_sumcheck;     /* 1 + initial_k messages (u0, u2) */
+    size_t n_fold_nonces;  /* rounds with fold_grinding_bits0 - j > 0 */
+    size_t n_queries;
+    size_t n_alpha;        /* ceil_log2(queries0) */
+    size_t row_len;        /* 2^initial_k elements per opened row */
+    size_t n_proof_hashes;
+    size_t folded_len;     /* 2^(log_msg_len - initial_k) */
+} bz_l0_sizes;
+typedef struct bz_l0_opening bz_l0_opening;
+/* d_packed / d_basis: 2^log_msg_len elements on the device (the packed
+ * witness and the combined basis b_initial); the transcript is advanced in
+ * place.  Both device arrays are only read. */
+int bz_ligerito_open_l0(bz_ctx *ctx, bz_transcript *transcript, bz_commitment *c0,
+                        const uint64_t *d_packed, const uint64_t *d_basis,
+                        const uint64_t target[2], const bz_l0_config *cfg,
+                        bz_l0_opening **out);
+int bz_l0_opening_sizes(const bz_l0_opening *o, bz_l0_sizes *sizes);
+/* Copy any subset of the results (NULL skips): sumcheck n_sumcheck x 4 words
+ * {u0.lo, u0.hi, u2.lo, u2.hi}; fold challenges initial_k x 2 words; alpha
+ * n_alpha x 2 words; rows n_queries x row_len x 2 words (row q = codeword
+ * positions q * row_len ...); proof n_proof_hashes x 32 bytes. */
+int bz_l0_opening_copy(const bz_l0_opening *o, uint64_t *sumcheck, uint64_t *fold_nonces,
+                       uint64_t *challenges, uint8_t root1[32], uint64_t *grinding_nonce,
+                       uint64_t *queries, uint64_t *alpha, uint64_t *rows, uint8_t *proof);
+/* The level-1 commitment (owned by the opening). */
+bz_commitment *bz_l0_opening_level1(bz_l0_opening *o);
+/* The folded witness f^1 and basis (device, owned by the opening). */
+int bz_l0_opening_folded(const bz_l0_opening *o, const uint64_t **d_f1, const uint64_t **d_b1,
+                         size_t *n1);
+int bz_l0_opening_free(bz_l0_opening *o);
 
 /* ---- synthetic inputs --------------------------------------------------- */
 /* RFC 8439 ChaCha20 keystream words (key = seed LE u64 zero padded, nonce 0,

@@ -523,6 +523,82 @@ void orc_blake3_hash(const uint8_t *data, size_t len, uint8_t out[32]) {
     cv_to_bytes(w, out);
 }
 
+/* Extended output (XOF) of the unkeyed hash: the root node -- the last block
+ * of a one-chunk input, else the top parent -- compressed with the ROOT flag
+ * and the output block index as its counter; every output block is all 16
+ * state words (the `blake3` crate's finalize_xof used by BitZ's
+ * Blake3Transcript, src/transcript/mod.rs:49-52). */
+void orc_blake3_xof(const uint8_t *data, size_t len, uint8_t *out, size_t out_len) {
+    uint32_t cv[8];
+    uint8_t blk[64];
+    uint32_t block_len, flags;
+    memset(blk, 0, 64);
+    if (len <= 1024) {
+        memcpy(cv, IV8, sizeof cv);
+        size_t nblocks = len == 0 ? 1 : (len + 63) / 64;
+        for (size_t b = 0; b + 1 < nblocks; ++b) {
+            uint32_t o[16];
+            b3_compress(cv, data + 64 * b, 0, 64, b == 0 ? B3_CHUNK_START : 0, o);
+            memcpy(cv, o, 32);
+        }
+        size_t off = 64 * (nblocks - 1);
+        block_len = (uint32_t)(len - off);
+        memcpy(blk, data + off, block_len);
+        flags = (nblocks == 1 ? B3_CHUNK_START : 0) | B3_CHUNK_END;
+    } else {
+        size_t n = (len + 1023) / 1024, left = 1;
+        while (left * 2 < n) left *= 2;
+        uint32_t l[8], r[8];
+        b3_subtree(data, left * 1024, 0, 0, l);
+        b3_subtree(data + left * 1024, len - left * 1024, left, 0, r);
+        memcpy(cv, IV8, sizeof cv);
+        cv_to_bytes(l, blk);
+        cv_to_bytes(r, blk + 32);
+        block_len = 64;
+        flags = B3_PARENT;
+    }
+    for (uint64_t t = 0; 64 * t < out_len; ++t) {
+        uint32_t o[16];
+        b3_compress(cv, blk, t, block_len, flags | B3_ROOT, o);
+        for (int i = 0; i < 64 && 64 * t + i < out_len; ++i)
+            out[64 * t + i] = (uint8_t)(o[i / 4] >> (8 * (i % 4)));
+    }
+}
+
+/* Proof of work (BitZ src/utils/blake3x4.rs:42-60): blake3(prefix || nonce_le)
+ * has at least `bits` leading zero bits, counted from the most significant bit
+ * of byte 0. */
+int orc_pow_ok(const uint8_t *prefix, size_t plen, uint64_t nonce, unsigned bits) {
+    uint8_t buf[64], h[32];
+    memcpy(buf, prefix, plen);
+    for (int i = 0; i < 8; ++i) buf[plen + i] = (uint8_t)(nonce >> (8 * i));
+    orc_blake3_hash(buf, plen + 8, h);
+    unsigned acc = 0;
+    for (int i = 0; i < 32; ++i) {
+        if (h[i] == 0) {
+            acc += 8;
+            continue;
+        }
+        unsigned b = h[i], lz = 0;
+        while (!(b & 0x80)) {
+            ++lz;
+            b <<= 1;
+        }
+        acc += lz;
+        break;
+    }
+    return acc >= bits;
+}
+
+/* The smallest nonce in [start, end) passing orc_pow_ok (serial scan,
+ * first_pow_nonce of blake3x4.rs); UINT64_MAX when none. */
+uint64_t orc_pow_first_nonce(const uint8_t *prefix, size_t plen, uint64_t start, uint64_t end,
+                             unsigned bits) {
+    for (uint64_t n = start; n < end; ++n)
+        if (orc_pow_ok(prefix, plen, n, bits)) return n;
+    return UINT64_MAX;
+}
+
 void orc_blake3_leaf_cv(const uint8_t *data, size_t len, uint8_t out[32]) {
     uint32_t w[8];
     b3_subtree(data, len, 0, 0, w);

@@ -57,6 +57,13 @@ void orc_blake3_leaf_cv(const uint8_t *data, size_t len, uint8_t out[32]);
 /* merge_subtrees_non_root(l, r, Mode::Hash) */
 void orc_blake3_parent_cv(const uint8_t l[32], const uint8_t r[32], uint8_t out[32]);
 
+/* BLAKE3 extended output (finalize_xof) of the whole input */
+void orc_blake3_xof(const uint8_t *data, size_t len, uint8_t *out, size_t out_len);
+/* proof of work: blake3(prefix || nonce_le) has >= bits leading zero bits */
+int orc_pow_ok(const uint8_t *prefix, size_t plen, uint64_t nonce, unsigned bits);
+uint64_t orc_pow_first_nonce(const uint8_t *prefix, size_t plen, uint64_t start, uint64_t end,
+                             unsigned bits);
+
 /* hash_kind: 0 = SHA-256, 1 = BLAKE3 */
 void orc_hash_leaf(const uint8_t *data, size_t len, int kind, uint8_t out[32]);
 void orc_hash_pair(const uint8_t l[32], const uint8_t r[32], int kind, uint8_t out[32]);

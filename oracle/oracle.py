@@ -59,6 +59,9 @@ def _declare(L):
         "orc_ntt_forward": (None, [_P, _I]),
         "orc_sha256": (None, [_P, _S, _P]),
         "orc_blake3_hash": (None, [_P, _S, _P]),
+        "orc_blake3_xof": (None, [_P, _S, _P, _S]),
+        "orc_pow_ok": (_I, [_P, _S, _U64, ctypes.c_uint]),
+        "orc_pow_first_nonce": (_U64, [_P, _S, _U64, _U64, ctypes.c_uint]),
         "orc_blake3_leaf_cv": (None, [_P, _S, _P]),
         "orc_blake3_parent_cv": (None, [_P, _P, _P]),
         "orc_hash_leaf": (None, [_P, _S, _I, _P]),
@@ -180,6 +183,26 @@ def blake3(data: bytes) -> bytes:
     out = np.zeros(32, np.uint8)
     lib().orc_blake3_hash(_p(a), len(data), _p(out))
     return out.tobytes()
+
+
+def blake3_xof(data: bytes, out_len: int) -> bytes:
+    a = _bytes_in(data)
+    out = np.zeros(max(out_len, 1), np.uint8)
+    lib().orc_blake3_xof(_p(a), len(data), _p(out), out_len)
+    return out[:out_len].tobytes()
+
+
+def pow_ok(prefix: bytes, nonce: int, bits: int) -> bool:
+    return bool(lib().orc_pow_ok(_p(_bytes_in(prefix)), len(prefix), nonce, bits))
+
+
+def pow_first_nonce(prefix: bytes, bits: int, start: int = 0, end: int = 2**64 - 1) -> int | None:
+    """Smallest nonce in [start, end) with blake3(prefix || nonce_le) having
+    ``bits`` leading zero bits (serial scan); None when there is none."""
+    if not 0 < len(prefix) + 8 <= 64:
+        raise ValueError("prefix + nonce must fit one 64-byte block")
+    n = lib().orc_pow_first_nonce(_p(_bytes_in(prefix)), len(prefix), start, end, bits)
+    return None if n == 2**64 - 1 else int(n)
 
 
 def blake3_leaf_cv(data: bytes) -> bytes:

@@ -1,0 +1,174 @@
+"""Oracle transcript, BLAKE3 extended output and proof of work (CPU).
+
+Pins:
+* BLAKE3 XOF of the empty input, 131 bytes -- the published BLAKE3 test
+  vector for input length 0 (the `blake3` crate's test_vectors.json, the
+  crate pinned by BitZ's Cargo.lock at 1.8.7); the first 32 bytes are the
+  32-byte hash already pinned in test_oracle_hash.py.
+* Framing and sampling behaviour the reference's own transcript tests check
+  (src/transcript/mod.rs:173-190): absorb_slice is length framed, and two
+  samplings from one state differ.
+* Proof of work: the found nonce passes and every smaller nonce fails
+  (first_pow_nonce, src/utils/blake3x4.rs:42-69), verify_pow accepts it and
+  rejects a failing one, zero bits gives nonce 0.
+"""
+import os
+import struct
+
+import numpy as np
+import pytest
+
+EMPTY_XOF_131 = (
+    "af1349b9f5f9a1a6a0404dea36dcc9499bcb25c9adc112b7cc9a93cae41f3262"
+    "e00f03e7b69af26b7faaf09fcd333050338ddfe085b8cc869ca98b206c08243a"
+    "26f5487789e8f660afe6c99ef9e0c52b92e7393024a80459cf91f476f9ffdbda"
+    "7001c22e159b402631f277ca96f2defdf1078282314e763699a31c5363165421"
+    "cce14d"
+)
+
+
+def test_blake3_xof_empty_kat(oracle):
+    assert oracle.blake3_xof(b"", 131).hex() == EMPTY_XOF_131
+
+
+@pytest.mark.parametrize("n", [0, 1, 63, 64, 65, 1023, 1024, 1025, 2048, 3072, 5000, 70000])
+def test_blake3_xof_prefix_is_hash(oracle, n):
+    d = np.random.default_rng(n).integers(0, 256, n, dtype=np.uint8).tobytes()
+    x = oracle.blake3_xof(d, 300)
+    assert x[:32] == oracle.blake3(d)
+    assert oracle.blake3_xof(d, 64) == x[:64]
+    assert oracle.blake3_xof(d, 65) == x[:65]
+
+
+def test_transcript_framing(oracle):
+    from oracle.transcript import Blake3Transcript
+
+    a, b = Blake3Transcript(), Blake3Transcript()
+    a.absorb_slice(bytes([1, 7, 6, 2]))
+    b.absorb_slice(bytes([1]))
+    b.absorb_slice(bytes([2]))
+    first = a.fill_sampling_bytes(16)
+    second = a.fill_sampling_bytes(16)
+    other = b.fill_sampling_bytes(16)
+    assert first != second and first != other
+    # absorb_slice is exactly 0x06 || len LE || data || 0x07
+    c = Blake3Transcript()
+    c.absorb(b"\x06" + struct.pack("<Q", 4) + bytes([1, 7, 6, 2]) + b"\x07")
+    a2 = Blake3Transcript()
+    a2.absorb_slice(bytes([1, 7, 6, 2]))
+    assert c.state_digest() == a2.state_digest()
+
+
+def test_transcript_challenge_replays(oracle):
+    from oracle.transcript import Blake3Transcript
+
+    a, b = Blake3Transcript(), Blake3Transcript()
+    for t in (a, b):
+        t.absorb_slice(b"label")
+    xs = [a.challenge_bytes(16) for _ in range(8)]
+    ys = [b.challenge_bytes(16) for _ in range(8)]
+    assert xs == ys and len(set(xs)) == 8
+    # a squeeze does not consume the state: digest is over absorbed bytes
+    c = Blake3Transcript()
+    c.absorb_slice(b"label")
+    out = c._xof(16)
+    assert out == Blake3Transcript.challenge_bytes(c.clone(), 16)
+
+
+@pytest.mark.parametrize("bits", [1, 4, 8, 12])
+@pytest.mark.parametrize("plen", [16, 24, 31, 32, 56])
+def test_pow_first_nonce_is_smallest(oracle, bits, plen):
+    prefix = bytes((7 * i + bits) & 0xFF for i in range(plen))
+    n = oracle.pow_first_nonce(prefix, bits)
+    assert n is not None and oracle.pow_ok(prefix, n, bits)
+    for m in range(n):
+        assert not oracle.pow_ok(prefix, m, bits)
+    # the serial scan from a later start finds the next passing nonce
+    n2 = oracle.pow_first_nonce(prefix, bits, start=n + 1)
+    assert n2 > n and oracle.pow_ok(prefix, n2, bits)
+
+
+def test_pow_bit_order(oracle):
+    # leading zeros are counted from the most significant bit of byte 0
+    prefix = b"\x00" * 16
+    for n in range(200):
+        h = oracle.blake3(prefix + struct.pack("<Q", n))
+        lz = 0
+        for byte in h:
+            if byte == 0:
+                lz += 8
+                continue
+            lz += 8 - byte.bit_length()
+            break
+        for bits in range(0, 12):
+            assert oracle.pow_ok(prefix, n, bits) == (lz >= bits)
+
+
+def test_challenger_grind_and_verify(oracle):
+    from oracle.transcript import Blake3Transcript, ZincChallenger
+
+    p = ZincChallenger(Blake3Transcript())
+    v = ZincChallenger(Blake3Transcript())
+    for ch in (p, v):
+        ch.observe_label(b"flock-ligerito-basis-v0")
+        ch.observe_f128([5, 6])
+    nonce = p.grind_pow(10)
+    assert v.verify_pow(nonce, 10)
+    assert p.t.state_digest() == v.t.state_digest()
+    assert p.grind_pow(0) == 0
+    assert v.verify_pow(0, 0)
+    assert p.sample_f128().tolist() == v.sample_f128().tolist()
+    # a wrong nonce is rejected and the states stay in lockstep
+    q = ZincChallenger(Blake3Transcript())
+    w = ZincChallenger(Blake3Transcript())
+    good = q.grind_pow(8)
+    bad = next(m for m in range(good + 1, good + 100000)
+               if not oracle.pow_ok(w.t.clone().challenge_bytes(16), m, 8))
+    assert not w.verify_pow(bad, 8)
+    assert not ZincChallenger(Blake3Transcript()).verify_pow(1, 0)
+
+
+def test_sample_distinct_queries(oracle):
+    from oracle.ligerito_l0 import ceil_log2, sample_distinct_queries
+    from oracle.transcript import Blake3Transcript, ZincChallenger
+
+    ch = ZincChallenger(Blake3Transcript())
+    qs = sample_distinct_queries(ch, 16, 16)
+    assert qs == list(range(16))
+    ch2 = ZincChallenger(Blake3Transcript())
+    qs2 = sample_distinct_queries(ch2, 1 << 14, 148)
+    assert qs2 == sorted(set(qs2)) and len(qs2) == 148
+    with pytest.raises(ValueError):
+        sample_distinct_queries(ch2, 4, 5)
+    assert [ceil_log2(n) for n in (0, 1, 2, 3, 4, 5, 148, 256)] == [0, 0, 1, 2, 2, 3, 8, 8]
+
+
+def test_oracle_l0_opening_consistency(oracle):
+    """The oracle's level-0 opening: its rows authenticate against the root,
+    its folds agree with partial_eval_lsb at the fold challenges, and the
+    first sumcheck message matches a direct round_msg_lsb."""
+    from oracle.ligerito_l0 import L0Config, open_l0
+    from oracle.transcript import Blake3Transcript, ZincChallenger
+
+    lm, r, k = 12, 2, 4
+    packed = oracle.chacha_words(3, 1 << lm)
+    basis = oracle.chacha_words(4, 1 << lm)
+    cw, tree, root = oracle.commit(packed, r, k, oracle.BLAKE3)
+    cfg = L0Config(initial_k=k, recursive_k0=3, log_inv_rate0=r, log_inv_rate1=2,
+                   fold_grinding_bits0=6, grinding_bits0=8, queries0=12)
+    res = open_l0(ZincChallenger(Blake3Transcript()), packed, basis, [9, 10], cw, tree, root, cfg)
+    assert len(res.sumcheck) == k + 1 and len(res.fold_nonces) == k
+    u0, u2 = oracle.round_msg_lsb(packed, basis)
+    assert (res.sumcheck[0][0] == u0).all() and (res.sumcheck[0][1] == u2).all()
+    rs = np.array(res.fold_challenges)
+    assert (oracle.partial_eval_lsb(packed, rs) == res.folded).all()
+    n_leaves = 1 << (lm - k + r)
+    leaf_hashes = np.array([np.frombuffer(oracle.hash_leaf(row.astype("<u8").tobytes(),
+                                                           oracle.BLAKE3), np.uint8)
+                            for row in res.opened_rows])
+    assert (leaf_hashes == tree[np.array(res.queries)]).all()
+    assert oracle.verify_merkle_multi_proof(root, n_leaves, res.queries, leaf_hashes,
+                                            res.merkle_proof, oracle.BLAKE3)
+    assert res.alpha.shape == (4, 2)
+    _, _, root1 = oracle.commit(res.folded, 2, 3, oracle.BLAKE3)
+    assert root1 == res.root1
