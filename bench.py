@@ -155,15 +155,26 @@ def _peaks():
 
 def cpu_baseline(n_threads: int, log_n: int = LOG_N):
     """The oracle commit (CPU restatement of the reference) on a full 2^24
-    commit with all host threads; elements per second."""
+    commit with all host threads; elements per second.  Also times the
+    oracle's level-0 opening of that commitment with the opening leg's
+    configuration (its folds run on one thread)."""
     from oracle import oracle as O
+    from oracle.ligerito_l0 import L0Config, open_l0
+    from oracle.transcript import Blake3Transcript, ZincChallenger
 
     O.build()
     msg = O.chacha_words(SEED, 1 << log_n)
     t0 = time.perf_counter()
-    _, _, root = O.commit(msg, LOG_INV_RATE, LOG_LANES, HASH, n_threads=n_threads)
+    cw, tree, root = O.commit(msg, LOG_INV_RATE, LOG_LANES, HASH, n_threads=n_threads)
     dt = time.perf_counter() - t0
-    return (1 << log_n) / dt, dt, root
+    basis = O.chacha_words(77, 1 << log_n)
+    t = Blake3Transcript()
+    t.absorb_slice(b"bench opening")
+    t1 = time.perf_counter()
+    open_l0(ZincChallenger(t), msg, basis, [1, 2], cw, tree, root,
+            L0Config(LOG_LANES, 6, LOG_INV_RATE, 2, 0, 16, 148, HASH))
+    open_ms = (time.perf_counter() - t1) * 1e3
+    return (1 << log_n) / dt, dt, root, open_ms
 
 
 def run_reference(args, ws, rank):
@@ -361,11 +372,12 @@ def run_gpu(args, ws, rank, local):
         cpu = None
         if not args.skip_cpu:
             threads = os.cpu_count() or 1
-            v, dt, croot = cpu_baseline(threads)
+            v, dt, croot, cpu_open_ms = cpu_baseline(threads)
             assert croot == root0 or rank != 0 or SEED + rank != SEED
             cpu = {"value": v, "unit": UNIT, "cores": threads, "kind": "port",
                    "sample": f"one full 2^24-element commit ({dt:.2f} s) by the CPU "
-                             "restatement of the reference on all host threads"}
+                             "restatement of the reference on all host threads",
+                   "open_l0_ms": cpu_open_ms}
         sorted_ms = sorted(step_ms)
         p99 = sorted_ms[min(len(sorted_ms) - 1, int(round(0.99 * (len(sorted_ms) - 1))))]
         out = {
@@ -482,35 +494,48 @@ def _bench_shapes(ctx, bz):
 
 
 def _bench_open(ctx, bz, msg, params):
-    """Opening leg at 2^24: the 12-round L0 lane fold of the committed
-    message against a basis polynomial (SumcheckProver.new + 12 folds), then
-    148 opened rows and their Merkle multi-proof from the resident commitment."""
+    """Opening leg at 2^24 (2^12 lanes x 2^12 columns, rate 1/4): the level-0
+    Ligerito opening of the resident commitment through bz_ligerito_open_l0 --
+    transcript prefix, first sumcheck message, 12 lane folds, the level-1
+    commit of the folded 2^12 elements (2^6 lanes, rate 1/4), a 16-bit query
+    grind, 148 distinct queries (the rate-1/4 unique-decoding count), alpha_0,
+    and the 148 opened rows with their Merkle multi-proof.  Host wall time of
+    the whole call (it synchronizes for every transcript squeeze).  Also times
+    the GPU proof-of-work search alone at 24 bits."""
     import numpy as np
-    from bitz_gb300.ligerito import SumcheckProver
 
-    rng = np.random.default_rng(12)
     b = bz.DeviceArray.chacha(77, msg.n, ctx)
     c, pd = bz.commit(msg, params, ctx)
-    rs = rng.integers(0, 2**64, (12, 2), dtype=np.uint64)
-    q = sorted(set(rng.integers(0, params.n_leaves(), 148).tolist()))
+    cfg = bz.L0Config(initial_k=params.log_batch_size, recursive_k0=6, log_inv_rate1=2,
+                      fold_grinding_bits0=0, grinding_bits0=16, queries0=148, hash_kind=1)
     times = []
-    for _ in range(3):
+    res = None
+    for i in range(4):
+        t = bz.Blake3Transcript()
+        t.absorb_slice(b"bench opening")
         ctx.synchronize()
         t0 = time.perf_counter()
-        prover, _ = SumcheckProver.new(msg, b, 0)
-        for r in rs:
-            prover.fold(r)
-        t1 = time.perf_counter()
-        rows = pd.rows(q)
-        proof = pd.multi_proof(q)
-        t2 = time.perf_counter()
-        times.append((t1 - t0, t2 - t1))
+        res = bz.open_l0(t, pd, msg, b, [1, 2], cfg, ctx)
+        times.append(time.perf_counter() - t0)
+        if i < 3:
+            res.free()
+    info = {"open_l0_ms": min(times[1:]) * 1e3, "open_l0_ms_median": statistics.median(times[1:]) * 1e3,
+            "queries": len(res.queries), "proof_hashes": int(len(res.merkle_proof)),
+            "row_bytes": int(res.opened_rows.nbytes), "grinding_nonce": res.grinding_nonce,
+            "config": "initial_k 12, recursive_k0 6, log_inv_rate1 2, fold_grinding_bits0 0, "
+                      "grinding_bits0 16, queries0 148, BLAKE3"}
+    res.free()
+    # proof-of-work search alone: hashes scanned >= smallest nonce + 1
+    pw = []
+    for seed in range(3):
+        prefix = bytes([seed]) * 16
+        t0 = time.perf_counter()
+        n = bz.pow_first_nonce(prefix, 24, ctx=ctx)
+        pw.append((n + 1) / (time.perf_counter() - t0))
+    info["pow_24bit_hashes_per_s_lower_bound"] = float(np.median(pw))
     pd.free()
     b.free()
-    fold_s, open_s = min(times)
-    return {"fold_12_rounds_ms": fold_s * 1e3, "queries": len(q),
-            "rows_and_multiproof_ms": open_s * 1e3, "proof_hashes": int(len(proof)),
-            "row_bytes": int(rows.nbytes)}
+    return info
 
 
 def _geometric_sizes(rng, n, lo=14, hi=26, q=0.97):

@@ -97,6 +97,28 @@ _SIGS = {
     "bz_l0_opening_level1": (_P, [_P]),
     "bz_l0_opening_folded": (_I, [_P, _PP, _PP, ctypes.POINTER(_S)]),
     "bz_l0_opening_free": (_I, [_P]),
+    "bz_ligerito_proof_encode": (_I, [_P, _P, _S, ctypes.POINTER(_S)]),
+    "bz_ligerito_proof_decode": (_I, [_P, _S, _PP]),
+    "bz_ligerito_proof_view_of": (_I, [_P, _P]),
+    "bz_ligerito_proof_free": (_I, [_P]),
+    "bz_writer_create": (_I, [_PP]),
+    "bz_writer_destroy": (_I, [_P]),
+    "bz_writer_len": (_I, [_P, _U64]),
+    "bz_writer_gf": (_I, [_P, _P]),
+    "bz_writer_bytes": (_I, [_P, _P, _S]),
+    "bz_writer_data": (_I, [_P, _P, ctypes.POINTER(_S)]),
+    "bz_write_round0": (_I, [_P, _P, _I, _U64]),
+    "bz_write_ring_switch": (_I, [_P, _P]),
+    "bz_write_ligerito": (_I, [_P, _P]),
+    "bz_reader_create": (_I, [_P, _S, _PP]),
+    "bz_reader_destroy": (_I, [_P]),
+    "bz_reader_remaining": (_S, [_P]),
+    "bz_reader_len": (_I, [_P, ctypes.POINTER(_U64)]),
+    "bz_reader_gf": (_I, [_P, _P]),
+    "bz_reader_take": (_I, [_P, _S, _P]),
+    "bz_read_round0": (_I, [_P, _P, ctypes.POINTER(_I), ctypes.POINTER(_U64)]),
+    "bz_read_ring_switch": (_I, [_P, _P]),
+    "bz_read_ligerito": (_I, [_P, _PP]),
     "bz_autotune": (_I, [_P, ctypes.POINTER(Params), _I, ctypes.POINTER(_U32)]),
     "bz_schedule_get": (_I, [_P, ctypes.POINTER(Params), ctypes.POINTER(_U32)]),
     "bz_schedule_set": (_I, [_P, ctypes.POINTER(Params), _U32]),

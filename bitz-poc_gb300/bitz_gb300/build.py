@@ -19,7 +19,7 @@ LIB = os.path.join(PKG, "libbitzgpu.so")
 INCLUDE = os.path.join(os.path.dirname(ROOT), "include")
 
 SOURCES = ["ntt.cu", "merkle.cu", "fold.cu", "runtime.cu", "batch.cu", "serve.cu", "pipeline.cu", "noalloc.cu",
-           "transcript.cu", "pow.cu", "open.cu"]
+           "transcript.cu", "pow.cu", "open.cu", "codec.cpp"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 FLAGS = ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "-Xcompiler", "-O2",
          "--expt-relaxed-constexpr"]
@@ -36,7 +36,7 @@ def _deps() -> list[str]:
     out = []
     for d in (CSRC, INCLUDE):
         for f in os.listdir(d):
-            if f.endswith((".cu", ".cuh", ".h")):
+            if f.endswith((".cu", ".cuh", ".h", ".cpp")):
                 out.append(os.path.join(d, f))
     return out
 

@@ -290,6 +290,9 @@ const char *bz_status_string(int s) {
         case BZ_ERR_TIMEOUT: return "timeout";
         case BZ_ERR_STATE: return "invalid state";
         case BZ_ERR_NOTFOUND: return "not found";
+        case BZ_ERR_TRUNCATED: return "proof stream truncated";
+        case BZ_ERR_NONCANONICAL: return "proof stream encoded non-minimally";
+        case BZ_ERR_DECODE: return "LigeritoProof decode failed";
         default: return "unknown status";
     }
 }

@@ -32,7 +32,11 @@ typedef enum {
     BZ_ERR_BUSY = 5,     /* server queue full */
     BZ_ERR_TIMEOUT = 6,  /* a bounded wait ran out */
     BZ_ERR_STATE = 7,    /* handle in the wrong state (e.g. opened twice, freed) */
-    BZ_ERR_NOTFOUND = 8  /* unknown request id; no proof-of-work nonce in the range */
+    BZ_ERR_NOTFOUND = 8, /* unknown request id; no proof-of-work nonce in the range */
+    /* proof codec (src/proof_codec.rs:14-25 CodecError) */
+    BZ_ERR_TRUNCATED = 9,    /* the stream ended before a field */
+    BZ_ERR_NONCANONICAL = 10, /* a field encoded non-minimally */
+    BZ_ERR_DECODE = 11       /* the bincode LigeritoProof blob does not decode */
 } bz_status;
 
 /* Merkle hash (flock-core/src/hash.rs:21-27; merkle.rs:203-232). */
@@ -361,6 +365,85 @@ bz_commitment *bz_l0_opening_level1(bz_l0_opening *o);
 int bz_l0_opening_folded(const bz_l0_opening *o, const uint64_t **d_f1, const uint64_t **d_b1,
                          size_t *n1);
 int bz_l0_opening_free(bz_l0_opening *o);
+
+/* ---- proof codec (host) ------------------------------------------------------ */
+/* flock's LigeritoProof (flock-core/src/pcs/ligerito.rs:1509-1551) as the
+ * bincode 1.3 fixed-int blob that BitZ embeds (src/binary_pcs.rs:527-544),
+ * and the BitZ proof stream around it (src/proof_codec.rs:39-161,
+ * binary_pcs.rs:487-557).  Rows are Vec<Vec<Gf128>>: n_rows lengths in
+ * row_lens and the rows' elements concatenated in data (2 words each). */
+typedef struct {
+    size_t n_rows;
+    const size_t *row_lens;
+    const uint64_t *data;
+} bz_rows_view;
+/* RecursiveProof {opened_rows, merkle_proof}; FinalProof adds yr. */
+typedef struct {
+    bz_rows_view rows;
+    size_t n_hashes;
+    const uint8_t *hashes; /* n_hashes x 32 */
+} bz_level_view;
+typedef struct {
+    uint8_t initial_root[32];
+    bz_level_view initial_proof;
+    size_t n_recursive_roots;
+    const uint8_t *recursive_roots; /* x 32 */
+    size_t n_recursive_proofs;
+    const bz_level_view *recursive_proofs;
+    size_t n_yr;
+    const uint64_t *yr;             /* final_proof.yr, x 2 words */
+    bz_level_view final_rows;       /* final_proof.opened_rows / merkle_proof */
+    size_t n_sumcheck;
+    const uint64_t *sumcheck;       /* {u_0.lo, u_0.hi, u_2.lo, u_2.hi} each */
+    size_t n_grinding_nonces;
+    const uint64_t *grinding_nonces;
+    size_t n_ood_values;
+    const uint64_t *ood_values;     /* x 2 words */
+    size_t n_fold_grinding_nonces;
+    const uint64_t *fold_grinding_nonces;
+} bz_ligerito_proof_view;
+typedef struct bz_ligerito_proof bz_ligerito_proof;
+/* bincode::serialize(&proof): *len receives the blob size; out may be NULL
+ * (size query), else it must hold cap >= *len bytes. */
+int bz_ligerito_proof_encode(const bz_ligerito_proof_view *view, uint8_t *out, size_t cap,
+                             size_t *len);
+/* bincode fixint decode bounded by len, trailing bytes rejected
+ * (BZ_ERR_DECODE on any failure). */
+int bz_ligerito_proof_decode(const uint8_t *blob, size_t len, bz_ligerito_proof **out);
+/* A view whose pointers live as long as the decoded proof. */
+int bz_ligerito_proof_view_of(const bz_ligerito_proof *p, bz_ligerito_proof_view *view);
+int bz_ligerito_proof_free(bz_ligerito_proof *p);
+
+/* Writer (proof_codec.rs:39-89): len = u64 LE, gf = lo LE || hi LE, bytes raw. */
+typedef struct bz_writer bz_writer;
+int bz_writer_create(bz_writer **out);
+int bz_writer_destroy(bz_writer *w);
+int bz_writer_len(bz_writer *w, uint64_t n);
+int bz_writer_gf(bz_writer *w, const uint64_t g[2]);
+int bz_writer_bytes(bz_writer *w, const uint8_t *data, size_t len);
+/* The accumulated bytes (valid until the next write or destroy). */
+int bz_writer_data(const bz_writer *w, const uint8_t **data, size_t *len);
+/* write_round0 (binary_pcs.rs:487-496): gf(y) || len(0) | len(1) || len(nonce). */
+int bz_write_round0(bz_writer *w, const uint64_t y[2], int has_nonce, uint64_t nonce);
+/* write_ring_switch (:510-519): the 128 partial evaluations s_v. */
+int bz_write_ring_switch(bz_writer *w, const uint64_t s_v[256]);
+/* write_ligerito (:527-531): len(blob) || blob. */
+int bz_write_ligerito(bz_writer *w, const bz_ligerito_proof_view *view);
+/* Reader (proof_codec.rs:91-161) over a caller buffer that must outlive it;
+ * BZ_ERR_TRUNCATED when a field runs past the end. */
+typedef struct bz_reader bz_reader;
+int bz_reader_create(const uint8_t *buf, size_t len, bz_reader **out);
+int bz_reader_destroy(bz_reader *r);
+size_t bz_reader_remaining(const bz_reader *r);
+int bz_reader_len(bz_reader *r, uint64_t *n);
+int bz_reader_gf(bz_reader *r, uint64_t g[2]);
+int bz_reader_take(bz_reader *r, size_t n, const uint8_t **data);
+/* read_round0 (:498-508): BZ_ERR_NONCANONICAL for a presence tag > 1. */
+int bz_read_round0(bz_reader *r, uint64_t y[2], int *has_nonce, uint64_t *nonce);
+int bz_read_ring_switch(bz_reader *r, uint64_t s_v[256]);
+/* read_ligerito (:533-544): BZ_ERR_TRUNCATED when the length exceeds
+ * 64 MiB or the bytes left; BZ_ERR_DECODE when the blob does not decode. */
+int bz_read_ligerito(bz_reader *r, bz_ligerito_proof **out);
 
 /* ---- synthetic inputs --------------------------------------------------- */
 /* RFC 8439 ChaCha20 keystream words (key = seed LE u64 zero padded, nonce 0,
