@@ -156,10 +156,10 @@ def _peaks():
 def cpu_baseline(n_threads: int, log_n: int = LOG_N):
     """The oracle commit (CPU restatement of the reference) on a full 2^24
     commit with all host threads; elements per second.  Also times the
-    oracle's level-0 opening of that commitment with the opening leg's
-    configuration (its folds run on one thread)."""
+    oracle's recursive Ligerito proof of that commitment with the opening
+    leg's configuration (its folds run on one thread)."""
     from oracle import oracle as O
-    from oracle.ligerito_l0 import L0Config, open_l0
+    from oracle.ligerito import LigeritoConfig, prove
     from oracle.transcript import Blake3Transcript, ZincChallenger
 
     O.build()
@@ -171,8 +171,8 @@ def cpu_baseline(n_threads: int, log_n: int = LOG_N):
     t = Blake3Transcript()
     t.absorb_slice(b"bench opening")
     t1 = time.perf_counter()
-    open_l0(ZincChallenger(t), msg, basis, [1, 2], cw, tree, root,
-            L0Config(LOG_LANES, 6, LOG_INV_RATE, 2, 0, 16, 148, HASH))
+    prove(ZincChallenger(t), LigeritoConfig(**open_config(LOG_LANES)), msg, basis, [1, 2], cw,
+          tree, root)
     open_ms = (time.perf_counter() - t1) * 1e3
     return (1 << log_n) / dt, dt, root, open_ms
 
@@ -377,7 +377,7 @@ def run_gpu(args, ws, rank, local):
             cpu = {"value": v, "unit": UNIT, "cores": threads, "kind": "port",
                    "sample": f"one full 2^24-element commit ({dt:.2f} s) by the CPU "
                              "restatement of the reference on all host threads",
-                   "open_l0_ms": cpu_open_ms}
+                   "prove_ms": cpu_open_ms}
         sorted_ms = sorted(step_ms)
         p99 = sorted_ms[min(len(sorted_ms) - 1, int(round(0.99 * (len(sorted_ms) - 1))))]
         out = {
@@ -493,38 +493,55 @@ def _bench_shapes(ctx, bz):
     return out
 
 
+def open_config(log_lanes: int) -> dict:
+    """The opening leg's ProverConfig for a 2^log_lanes x 2^log_lanes witness."""
+    return dict(initial_k=log_lanes, recursive_ks=[log_lanes // 2],
+                log_inv_rates=[LOG_INV_RATE, 2], queries=[148, 148], grinding_bits=[16, 16],
+                fold_grinding_bits=None, ood_samples=None, hash_kind=HASH)
+
+
+
+OPEN_CONFIG_TEXT = ("recursive Ligerito, initial_k a, recursive_ks [a/2], log_inv_rates [2, 2], "
+                    "queries [148, 148] (the rate-1/4 unique-decoding count), grinding_bits "
+                    "[16, 16], no fold grinding, no OOD samples, BLAKE3")
+
+
 def _bench_open(ctx, bz, msg, params):
-    """Opening leg at 2^24 (2^12 lanes x 2^12 columns, rate 1/4): the level-0
-    Ligerito opening of the resident commitment through bz_ligerito_open_l0 --
-    transcript prefix, first sumcheck message, 12 lane folds, the level-1
-    commit of the folded 2^12 elements (2^6 lanes, rate 1/4), a 16-bit query
-    grind, 148 distinct queries (the rate-1/4 unique-decoding count), alpha_0,
-    and the 148 opened rows with their Merkle multi-proof.  Host wall time of
-    the whole call (it synchronizes for every transcript squeeze).  Also times
-    the GPU proof-of-work search alone at 24 bits."""
+    """Opening leg at 2^24 (2^12 lanes x 2^12 columns, rate 1/4): the whole
+    recursive Ligerito proof of the resident commitment through
+    bz_ligerito_prove (open_config), and its level-0 part alone through
+    bz_ligerito_open_l0.  Host wall time of each call (they synchronize for
+    every transcript squeeze), median of 3 after one warm-up.  Also times the
+    GPU proof-of-work search alone at 24 bits."""
     import numpy as np
+
+    from bitz_gb300 import codec
 
     b = bz.DeviceArray.chacha(77, msg.n, ctx)
     c, pd = bz.commit(msg, params, ctx)
-    cfg = bz.L0Config(initial_k=params.log_batch_size, recursive_k0=6, log_inv_rate1=2,
-                      fold_grinding_bits0=0, grinding_bits0=16, queries0=148, hash_kind=1)
-    times = []
-    res = None
-    for i in range(4):
-        t = bz.Blake3Transcript()
-        t.absorb_slice(b"bench opening")
-        ctx.synchronize()
-        t0 = time.perf_counter()
-        res = bz.open_l0(t, pd, msg, b, [1, 2], cfg, ctx)
-        times.append(time.perf_counter() - t0)
-        if i < 3:
-            res.free()
-    info = {"open_l0_ms": min(times[1:]) * 1e3, "open_l0_ms_median": statistics.median(times[1:]) * 1e3,
-            "queries": len(res.queries), "proof_hashes": int(len(res.merkle_proof)),
-            "row_bytes": int(res.opened_rows.nbytes), "grinding_nonce": res.grinding_nonce,
-            "config": "initial_k 12, recursive_k0 6, log_inv_rate1 2, fold_grinding_bits0 0, "
-                      "grinding_bits0 16, queries0 148, BLAKE3"}
-    res.free()
+    cfg = bz.LigeritoConfig(**open_config(params.log_batch_size))
+
+    def timed(fn, reps=4):
+        ts, out = [], None
+        for _ in range(reps):
+            t = bz.Blake3Transcript()
+            t.absorb_slice(b"bench opening")
+            ctx.synchronize()
+            t0 = time.perf_counter()
+            out = fn(t)
+            ts.append(time.perf_counter() - t0)
+            if hasattr(out, "free"):
+                out.free()
+        return statistics.median(ts[1:]) * 1e3, min(ts[1:]) * 1e3, out
+
+    prove_ms, prove_min, proof = timed(lambda t: bz.prove(t, pd, msg, b, [1, 2], cfg, ctx))
+    blob = codec.encode_ligerito(proof)
+    l0_cfg = bz.L0Config(initial_k=params.log_batch_size,
+                         recursive_k0=params.log_batch_size // 2, log_inv_rate1=2,
+                         grinding_bits0=16, queries0=148, hash_kind=HASH)
+    l0_ms, l0_min, _ = timed(lambda t: bz.open_l0(t, pd, msg, b, [1, 2], l0_cfg, ctx))
+    info = {"prove_ms": prove_ms, "prove_ms_min": prove_min, "proof_bytes": len(blob),
+            "open_l0_ms": l0_ms, "open_l0_ms_min": l0_min, "config": OPEN_CONFIG_TEXT}
     # proof-of-work search alone: hashes scanned >= smallest nonce + 1
     pw = []
     for seed in range(3):

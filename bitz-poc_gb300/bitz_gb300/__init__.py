@@ -22,4 +22,5 @@ from .pcs import (  # noqa: F401
     ligero_commit,
 )
 from .transcript import Blake3Transcript, ZincChallenger, blake3_xof, pow_first_nonce  # noqa: F401,E402
-from .opening import L0Config, L0Opening, open_l0  # noqa: F401,E402
+from .opening import L0Config, L0Opening, LigeritoConfig, open_l0, prove  # noqa: F401,E402
+from . import codec  # noqa: F401,E402

@@ -97,6 +97,8 @@ _SIGS = {
     "bz_l0_opening_level1": (_P, [_P]),
     "bz_l0_opening_folded": (_I, [_P, _PP, _PP, ctypes.POINTER(_S)]),
     "bz_l0_opening_free": (_I, [_P]),
+    "bz_l0_opening_ood_values": (_I, [_P, _P]),
+    "bz_ligerito_prove": (_I, [_P, _P, _P, _P, _P, _P, _P, _PP]),
     "bz_ligerito_proof_encode": (_I, [_P, _P, _S, ctypes.POINTER(_S)]),
     "bz_ligerito_proof_decode": (_I, [_P, _S, _PP]),
     "bz_ligerito_proof_view_of": (_I, [_P, _P]),

@@ -1,6 +1,9 @@
-"""Level-0 Ligerito opening against a device-resident commitment.
+"""Ligerito opening against a device-resident commitment.
 
-``open_l0`` runs the level-0 part of recursive_prover_with_basis_initial_impl
+``prove`` runs the whole recursive prover (recursive_prover_with_basis,
+flock-core/src/pcs/ligerito.rs:3455-3884) through ``bz_ligerito_prove`` and
+returns the LigeritoProof (codec.LigeritoProof).  ``open_l0`` runs the
+level-0 part of recursive_prover_with_basis_initial_impl
 (flock-core/src/pcs/ligerito.rs:3566-3720) through ``bz_ligerito_open_l0``:
 the transcript prefix, the lane folds with their grinding, the level-1
 ligero_commit of the folded witness, the query grind, the distinct queries
@@ -25,12 +28,13 @@ _S = ctypes.c_size_t
 class L0ConfigC(ctypes.Structure):
     _fields_ = [("initial_k", _U32), ("recursive_k0", _U32), ("log_inv_rate1", _U32),
                 ("fold_grinding_bits0", _U32), ("grinding_bits0", _U32), ("queries0", _U32),
-                ("hash_kind", _U32)]
+                ("hash_kind", _U32), ("ood_samples1", _U32)]
 
 
 class L0SizesC(ctypes.Structure):
     _fields_ = [("n_sumcheck", _S), ("n_fold_nonces", _S), ("n_queries", _S), ("n_alpha", _S),
-                ("row_len", _S), ("n_proof_hashes", _S), ("folded_len", _S)]
+                ("row_len", _S), ("n_proof_hashes", _S), ("folded_len", _S),
+                ("n_ood_values", _S)]
 
 
 @dataclass
@@ -45,11 +49,12 @@ class L0Config:
     grinding_bits0: int = 0
     queries0: int = 8
     hash_kind: int = 1
+    ood_samples1: int = 0
 
     def to_c(self) -> L0ConfigC:
         return L0ConfigC(self.initial_k, self.recursive_k0, self.log_inv_rate1,
                          self.fold_grinding_bits0, self.grinding_bits0, self.queries0,
-                         self.hash_kind)
+                         self.hash_kind, self.ood_samples1)
 
 
 class L0Opening:
@@ -84,6 +89,9 @@ class L0Opening:
         self.alpha = al[:sz.n_alpha].copy()
         self.opened_rows = rows[:sz.n_queries].copy()
         self.merkle_proof = proof[:sz.n_proof_hashes].copy()
+        ov = np.zeros((max(sz.n_ood_values, 1), 2), np.uint64)
+        check(ctx.handle, lib().bz_l0_opening_ood_values(handle, ptr(ov)))
+        self.ood_values = ov[:sz.n_ood_values].copy()
 
     def folded(self) -> tuple[int, int, int]:
         """Device pointers of f^1 and the folded basis, and their length."""
@@ -122,3 +130,60 @@ def open_l0(transcript: Blake3Transcript, data: ProverData, packed: DeviceArray,
                                                 packed.ptr, basis.ptr, ptr(t), ctypes.byref(c),
                                                 ctypes.byref(h)))
     return L0Opening(h, ctx)
+
+
+class LigeritoConfigC(ctypes.Structure):
+    _fields_ = [("initial_k", _U32), ("recursive_steps", _U32),
+                ("recursive_ks", ctypes.POINTER(_U32)), ("log_inv_rates", ctypes.POINTER(_U32)),
+                ("queries", ctypes.POINTER(_U32)), ("grinding_bits", ctypes.POINTER(_U32)),
+                ("fold_grinding_bits", ctypes.POINTER(_U32)),
+                ("ood_samples", ctypes.POINTER(_U32)), ("hash_kind", _U32)]
+
+
+@dataclass
+class LigeritoConfig:
+    """ProverConfig (ligerito.rs:124-160): recursive_ks has one entry per
+    recursive step, the other lists one more (level 0 first)."""
+    initial_k: int
+    recursive_ks: list
+    log_inv_rates: list
+    queries: list
+    grinding_bits: list
+    fold_grinding_bits: list | None = None
+    ood_samples: list | None = None
+    hash_kind: int = 1
+
+    def to_c(self):
+        r = len(self.recursive_ks)
+        keep = []
+
+        def arr(v, n):
+            if v is None:
+                return None
+            if len(v) != n:
+                raise ValueError("config list of the wrong length")
+            a = (_U32 * n)(*v)
+            keep.append(a)
+            return ctypes.cast(a, ctypes.POINTER(_U32))
+
+        c = LigeritoConfigC(self.initial_k, r, arr(self.recursive_ks, r),
+                            arr(self.log_inv_rates, r + 1), arr(self.queries, r + 1),
+                            arr(self.grinding_bits, r + 1), arr(self.fold_grinding_bits, r + 1),
+                            arr(self.ood_samples, r + 1), self.hash_kind)
+        return c, keep
+
+
+def prove(transcript: Blake3Transcript, data: ProverData, packed: DeviceArray,
+          basis: DeviceArray, target, cfg: LigeritoConfig, ctx: Context | None = None):
+    """The LigeritoProof of ``target`` against the commitment in ``data``."""
+    from .codec import _decoded
+
+    ctx = ctx or data.ctx or default_context()
+    t = np.ascontiguousarray(np.asarray(target, dtype=np.uint64).reshape(2))
+    c, keep = cfg.to_c()
+    h = ctypes.c_void_p()
+    check(ctx.handle, lib().bz_ligerito_prove(ctx.handle, transcript.handle, data._h(),
+                                              packed.ptr, basis.ptr, ptr(t), ctypes.byref(c),
+                                              ctypes.byref(h)))
+    del keep
+    return _decoded(h)

@@ -125,6 +125,19 @@ int launch_phi(const uint4 *d_eq_hi, size_t n, const uint4 *d_eq_r2, uint4 *d_ou
 int launch_chacha(uint64_t seed, uint64_t first_word, uint4 *d_out, size_t n_words,
                   cudaStream_t st);
 
+// Recursive Ligerito prover (ligerito.cu).  Induce: zero the 2^log_d domain,
+// scatter the nq query weights d_w at d_pos, apply the transposed forward NTT
+// with the twiddle heap of log_d; the low 2^log_msg_cols outputs are the
+// induced basis.
+int launch_induce_basis(uint4 *d_domain, int log_d, const uint64_t *d_pos, const uint4 *d_w,
+                        int nq, const uint4 *d_tw, cudaStream_t st);
+// d_b[j] += beta * d_nb[j]
+int launch_glue(uint4 *d_b, const uint4 *d_nb, size_t n, uint4 beta, cudaStream_t st);
+// d_out[0] = sum_j d_f[j] * d_b[j]; d_partial holds dot_partials_count(n) elements.
+size_t dot_partials_count(size_t n, int num_sms);
+int launch_dot(const uint4 *d_f, const uint4 *d_b, size_t n, uint4 *d_partial, uint4 *d_out,
+               cudaStream_t st, int num_sms);
+
 // One-time kernel attributes (large dynamic shared memory), called when a
 // context is created so no attribute call happens during graph capture.
 void init_ntt_kernels();

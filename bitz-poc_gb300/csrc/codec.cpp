@@ -16,20 +16,14 @@
 #include <vector>
 
 #include "../../include/bitz_gpu.h"
+#include "proof.h"
 
 namespace {
 
+using bzp::Level;
+using bzp::Rows;
+
 constexpr uint64_t kMaxProofBytes = 64ull << 20;  // binary_pcs.rs:63
-
-struct Rows {
-    std::vector<size_t> lens;
-    std::vector<uint64_t> data;  // concatenated rows, 2 words per element
-};
-
-struct Level {
-    Rows rows;
-    std::vector<uint8_t> hashes;  // 32 bytes each
-};
 
 void put_u64(std::vector<uint8_t> &o, uint64_t v) {
     for (int i = 0; i < 8; ++i) o.push_back((uint8_t)(v >> (8 * i)));
@@ -130,20 +124,6 @@ bz_rows_view rows_view(const Rows &r) {
 
 }  // namespace
 
-struct bz_ligerito_proof {
-    uint8_t initial_root[32];
-    Level initial;
-    std::vector<uint8_t> recursive_roots;
-    std::vector<Level> recursive;
-    std::vector<bz_level_view> recursive_views;
-    std::vector<uint64_t> yr;
-    Level fin;
-    std::vector<uint64_t> sumcheck;
-    std::vector<uint64_t> grinding_nonces;
-    std::vector<uint64_t> ood_values;
-    std::vector<uint64_t> fold_grinding_nonces;
-};
-
 struct bz_writer {
     std::vector<uint8_t> buf;
 };
@@ -210,13 +190,6 @@ int decode_blob(const uint8_t *blob, size_t len, bz_ligerito_proof **out) {
         delete p;
         return BZ_ERR_DECODE;
     }
-    for (const Level &l : p->recursive) {
-        bz_level_view v;
-        v.rows = rows_view(l.rows);
-        v.n_hashes = l.hashes.size() / 32;
-        v.hashes = l.hashes.data();
-        p->recursive_views.push_back(v);
-    }
     *out = p;
     return BZ_OK;
 }
@@ -244,8 +217,16 @@ int bz_ligerito_proof_decode(const uint8_t *blob, size_t len, bz_ligerito_proof 
     return decode_blob(blob, len, out);
 }
 
-int bz_ligerito_proof_view_of(const bz_ligerito_proof *p, bz_ligerito_proof_view *v) {
+int bz_ligerito_proof_view_of(bz_ligerito_proof *p, bz_ligerito_proof_view *v) {
     if (!p || !v) return BZ_ERR_ARG;
+    p->recursive_views.clear();
+    for (const Level &l : p->recursive) {
+        bz_level_view lv;
+        lv.rows = rows_view(l.rows);
+        lv.n_hashes = l.hashes.size() / 32;
+        lv.hashes = l.hashes.data();
+        p->recursive_views.push_back(lv);
+    }
     memcpy(v->initial_root, p->initial_root, 32);
     v->initial_proof.rows = rows_view(p->initial.rows);
     v->initial_proof.n_hashes = p->initial.hashes.size() / 32;

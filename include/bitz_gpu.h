@@ -57,6 +57,7 @@ typedef struct {
 
 typedef struct bz_ctx bz_ctx;
 typedef struct bz_commitment bz_commitment; /* device-resident ProverData + root */
+typedef struct bz_ligerito_proof bz_ligerito_proof; /* flock's LigeritoProof, host side */
 
 /* ---- context ---------------------------------------------------------- */
 const char *bz_status_string(int status);
@@ -323,8 +324,7 @@ int bz_transcript_verify_pow(bz_transcript *t, uint64_t nonce, uint32_t bits, in
  * transcript prefix, the initial_k lane folds (with fold grinding), the
  * level-1 ligero_commit of the folded witness, the query grind, the sampled
  * queries and alpha_0, and the opened rows with their Merkle multi-proof.
- * Requires initial_k == the commitment's log_batch_size and no level-1 OOD
- * samples (ood_samples[1] == 0). */
+ * Requires initial_k == the commitment's log_batch_size (>= 1). */
 typedef struct {
     uint32_t initial_k;           /* ProverConfig::initial_k */
     uint32_t recursive_k0;        /* recursive_ks[0] */
@@ -333,6 +333,7 @@ typedef struct {
     uint32_t grinding_bits0;      /* grinding_bits[0] */
     uint32_t queries0;            /* queries[0] */
     uint32_t hash_kind;           /* merkle_hash of the level-1 commitment */
+    uint32_t ood_samples1;        /* ood_samples[1]: OOD rounds after the level-1 root */
 } bz_l0_config;
 typedef struct {
     size_t n_sumcheck;     /* 1 + initial_k messages (u0, u2) */
@@ -342,6 +343,7 @@ typedef struct {
     size_t row_len;        /* 2^initial_k elements per opened row */
     size_t n_proof_hashes;
     size_t folded_len;     /* 2^(log_msg_len - initial_k) */
+    size_t n_ood_values;   /* ood_samples1 claimed evaluations */
 } bz_l0_sizes;
 typedef struct bz_l0_opening bz_l0_opening;
 /* d_packed / d_basis: 2^log_msg_len elements on the device (the packed
@@ -359,12 +361,41 @@ int bz_l0_opening_sizes(const bz_l0_opening *o, bz_l0_sizes *sizes);
 int bz_l0_opening_copy(const bz_l0_opening *o, uint64_t *sumcheck, uint64_t *fold_nonces,
                        uint64_t *challenges, uint8_t root1[32], uint64_t *grinding_nonce,
                        uint64_t *queries, uint64_t *alpha, uint64_t *rows, uint8_t *proof);
+/* ood_samples1 x 2 words: the claimed evaluations, in transcript order. */
+int bz_l0_opening_ood_values(const bz_l0_opening *o, uint64_t *values);
 /* The level-1 commitment (owned by the opening). */
 bz_commitment *bz_l0_opening_level1(bz_l0_opening *o);
 /* The folded witness f^1 and basis (device, owned by the opening). */
 int bz_l0_opening_folded(const bz_l0_opening *o, const uint64_t **d_f1, const uint64_t **d_b1,
                          size_t *n1);
 int bz_l0_opening_free(bz_l0_opening *o);
+
+/* ---- full recursive Ligerito opening ------------------------------------- */
+/* recursive_prover_with_basis / _initial (flock-core/src/pcs/ligerito.rs:
+ * 3455-3884) against a device-resident level-0 commitment: the level-0
+ * opening above, then every recursive level -- basis induction from the
+ * previous level's queries, introduce + glue, the level's folds, the next
+ * ligero_commit with its OOD rounds, grind, queries and opened rows -- and
+ * the final level's yr, grind and rows.  *out is the LigeritoProof
+ * (bz_ligerito_proof_view_of / bz_ligerito_proof_encode read it; free it with
+ * bz_ligerito_proof_free).  Array lengths follow ProverConfig
+ * (ligerito.rs:124-160): recursive_ks has recursive_steps entries, the
+ * others recursive_steps + 1; fold_grinding_bits / ood_samples may be NULL
+ * (all zero). */
+typedef struct {
+    uint32_t initial_k;
+    uint32_t recursive_steps;
+    const uint32_t *recursive_ks;
+    const uint32_t *log_inv_rates;      /* [0] must be the commitment's rate */
+    const uint32_t *queries;
+    const uint32_t *grinding_bits;
+    const uint32_t *fold_grinding_bits;
+    const uint32_t *ood_samples;        /* [0] must be 0 */
+    uint32_t hash_kind;                 /* merkle_hash of the recursive commitments */
+} bz_ligerito_config;
+int bz_ligerito_prove(bz_ctx *ctx, bz_transcript *transcript, bz_commitment *c0,
+                      const uint64_t *d_packed, const uint64_t *d_basis, const uint64_t target[2],
+                      const bz_ligerito_config *cfg, bz_ligerito_proof **out);
 
 /* ---- proof codec (host) ------------------------------------------------------ */
 /* flock's LigeritoProof (flock-core/src/pcs/ligerito.rs:1509-1551) as the
@@ -402,7 +433,6 @@ typedef struct {
     size_t n_fold_grinding_nonces;
     const uint64_t *fold_grinding_nonces;
 } bz_ligerito_proof_view;
-typedef struct bz_ligerito_proof bz_ligerito_proof;
 /* bincode::serialize(&proof): *len receives the blob size; out may be NULL
  * (size query), else it must hold cap >= *len bytes. */
 int bz_ligerito_proof_encode(const bz_ligerito_proof_view *view, uint8_t *out, size_t cap,
@@ -410,8 +440,9 @@ int bz_ligerito_proof_encode(const bz_ligerito_proof_view *view, uint8_t *out, s
 /* bincode fixint decode bounded by len, trailing bytes rejected
  * (BZ_ERR_DECODE on any failure). */
 int bz_ligerito_proof_decode(const uint8_t *blob, size_t len, bz_ligerito_proof **out);
-/* A view whose pointers live as long as the decoded proof. */
-int bz_ligerito_proof_view_of(const bz_ligerito_proof *p, bz_ligerito_proof_view *view);
+/* A view whose pointers live as long as the proof (and stay valid until the
+ * next view_of call on it). */
+int bz_ligerito_proof_view_of(bz_ligerito_proof *p, bz_ligerito_proof_view *view);
 int bz_ligerito_proof_free(bz_ligerito_proof *p);
 
 /* Writer (proof_codec.rs:39-89): len = u64 LE, gf = lo LE || hi LE, bytes raw. */

@@ -857,6 +857,79 @@ void orc_build_eq_lsb(const uint64_t *point, size_t k, uint64_t *out) {
     }
 }
 
+/* s_{i+1}(x) = s_i(x)^2 + s_i(v_i) s_i(x)  (ligerito.rs:1712-1715) */
+static void next_s(const uint64_t s[2], const uint64_t s_root[2], uint64_t out[2]) {
+    uint64_t a[2], b[2];
+    gf_mul(s, s, a);
+    gf_mul(s_root, s, b);
+    out[0] = a[0] ^ b[0];
+    out[1] = a[1] ^ b[1];
+}
+
+/* The basis a level's queries induce, in the dense form of
+ * induce_sumcheck_poly (flock-core/src/pcs/ligerito.rs:1968-2072):
+ * basis[j] = sum_i w[i] * W^_j(q_i), where W^_j(x) = prod_{k: bit_k(j)} W^_k(x)
+ * are the normalized LCH novel-basis polynomials at the field element q_i
+ * (= Gf128::new(q_i, 0)); s_k(v_k) from eval_sk_at_vks (:1720-1747), the
+ * products as evaluate_scaled_basis_inplace (:1749-1785). */
+void orc_induce_basis(int log_n, const uint64_t *queries, size_t nq, const uint64_t *w,
+                      uint64_t *basis) {
+    const size_t n = (size_t)1 << log_n;
+    uint64_t sks_vks[2 * 65], inv[2 * 65];
+    memset(sks_vks, 0, sizeof sks_vks);
+    sks_vks[0] = 1;
+    uint64_t layer[2 * 64];
+    for (int i = 1; i <= log_n; ++i) {
+        layer[2 * (i - 1)] = (uint64_t)1 << i;
+        layer[2 * (i - 1) + 1] = 0;
+    }
+    int cur_len = log_n;
+    for (int i = 0; i < log_n; ++i) {
+        for (int j = 0; j < cur_len; ++j) {
+            uint64_t t[2];
+            next_s(layer + 2 * j, sks_vks + 2 * i, t);
+            if (j == 0) {
+                sks_vks[2 * (i + 1)] = t[0];
+                sks_vks[2 * (i + 1) + 1] = t[1];
+            } else {
+                layer[2 * (j - 1)] = t[0];
+                layer[2 * (j - 1) + 1] = t[1];
+            }
+        }
+        --cur_len;
+    }
+    for (int k = 0; k <= log_n; ++k) {
+        if (sks_vks[2 * k] | sks_vks[2 * k + 1])
+            orc_gf_inv(sks_vks + 2 * k, inv + 2 * k);
+        else
+            inv[2 * k] = inv[2 * k + 1] = 0;
+    }
+    memset(basis, 0, 16 * n);
+    uint64_t *local = (uint64_t *)malloc(16 * n);
+    uint64_t sx[2 * 64];
+    for (size_t qi = 0; qi < nq; ++qi) {
+        if (log_n > 0) {
+            sx[0] = queries[qi];
+            sx[1] = 0;
+            for (int i = 1; i < log_n; ++i) next_s(sx + 2 * (i - 1), sks_vks + 2 * (i - 1), sx + 2 * i);
+            for (int i = 0; i < log_n; ++i) {
+                uint64_t t[2];
+                gf_mul(sx + 2 * i, inv + 2 * i, t);
+                sx[2 * i] = t[0];
+                sx[2 * i + 1] = t[1];
+            }
+        }
+        local[0] = w[2 * qi];
+        local[1] = w[2 * qi + 1];
+        for (int k = 0; k < log_n; ++k) {
+            const size_t len = (size_t)1 << k;
+            for (size_t i = 0; i < len; ++i) gf_mul(sx + 2 * k, local + 2 * i, local + 2 * (i + len));
+        }
+        for (size_t j = 0; j < 2 * n; ++j) basis[j] ^= local[j];
+    }
+    free(local);
+}
+
 /* sv_fold_mfr (src/ligerito.rs:317-375) by its defining identity:
  * s[j] = sum_y eq[y] * bit_j(P[y]). */
 void orc_sv_fold(const uint64_t *packed, size_t n, const uint64_t *eq, uint64_t *sv) {

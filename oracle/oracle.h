@@ -106,6 +106,11 @@ void orc_chacha_words(uint64_t seed, uint64_t first_word, uint64_t *out, size_t 
 void orc_chacha20_block(const uint32_t key[8], uint32_t counter, const uint32_t nonce[3],
                         uint8_t out[64]);
 
+/* ---- recursive opening ---- */
+/* dense induced basis of a level's queries (ligerito.rs:1968-2072) */
+void orc_induce_basis(int log_n, const uint64_t *queries, size_t nq, const uint64_t *w,
+                      uint64_t *basis);
+
 #ifdef __cplusplus
 }
 #endif

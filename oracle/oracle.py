@@ -74,6 +74,7 @@ def _declare(L):
         "orc_round_msg_lsb": (None, [_P, _P, _S, _P, _P]),
         "orc_fold_and_msg_lsb": (None, [_P, _P, _S, _P, _P, _P, _P, _P]),
         "orc_build_eq_lsb": (None, [_P, _S, _P]),
+        "orc_induce_basis": (None, [_I, _P, _S, _P, _P]),
         "orc_sv_fold": (None, [_P, _S, _P, _P]),
         "orc_phi_from_words": (None, [_P, _S, _P, _P]),
         "orc_chacha_words": (None, [_U64, _U64, _P, _S]),
@@ -305,6 +306,17 @@ def fold_and_msg_lsb(f: np.ndarray, b: np.ndarray, r):
     lib().orc_fold_and_msg_lsb(_p(f), _p(b), f.shape[0], _p(gf(r)), _p(nf), _p(nb), _p(u0),
                                _p(u2))
     return nf, nb, u0, u2
+
+
+def induce_basis(log_n: int, queries, weights) -> np.ndarray:
+    """Dense induced basis: sum_i weights[i] * W^_j(queries[i]) for j < 2^log_n."""
+    q = np.ascontiguousarray(np.asarray(queries, dtype=np.uint64))
+    w = np.ascontiguousarray(np.asarray(weights, dtype=np.uint64).reshape(-1, 2))
+    assert w.shape[0] == q.shape[0]
+    out = np.zeros((1 << log_n, 2), np.uint64)
+    lib().orc_induce_basis(log_n, _p(q) if len(q) else None, len(q), _p(w) if len(q) else None,
+                           _p(out))
+    return out
 
 
 def build_eq_lsb(point: np.ndarray) -> np.ndarray:

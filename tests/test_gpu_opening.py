@@ -184,3 +184,85 @@ def test_open_l0_c2_shape(oracle, ctx):
     """The 2^24-element witness (2^12 lanes x 2^12 columns, rate 1/4) opened
     with 12 lane folds, the shape of the benchmark's opening."""
     _run_l0(oracle, ctx, (24, 2, 12, 6, 2, 16, 16, 148, 1), seed=1)
+
+
+PROVE_CASES = [
+    # (log_n, rate0, initial_k, recursive_ks, log_inv_rates, queries, grinding, fold_grinding,
+    #  ood, hash)
+    (10, 1, 2, [2], [1, 1], [4, 3], [0, 0], None, None, 1),
+    (12, 2, 4, [3, 2], [2, 2, 1], [10, 6, 5], [4, 3, 2], [3, 2, 0], [0, 1, 2], 1),
+    (12, 2, 6, [2], [2, 2], [40, 12], [0, 6], [8, 0], [0, 1], 0),
+    (14, 2, 7, [3, 2], [2, 2, 2], [64, 30, 20], [8, 6, 4], None, [0, 0, 1], 1),
+    (16, 2, 8, [4], [2, 2], [148, 60], [12, 10], [10, 6], None, 1),
+]
+
+
+def _prove_both(oracle, ctx, case, seed):
+    from bitz_gb300 import (Blake3Transcript, DeviceArray, LigeritoConfig, PcsParams, codec,
+                            commit, prove)
+    from oracle import codec as OC
+    from oracle.ligerito import LigeritoConfig as OCfg, prove as oprove
+    from oracle.transcript import Blake3Transcript as OT, ZincChallenger as OZ
+
+    lm, r0, k, ks, rates, qs, gb, fb, ood, kind = case
+    packed = oracle.chacha_words(seed, 1 << lm)
+    basis = oracle.chacha_words(seed + 50, 1 << lm)
+    target = [seed, seed * 3 + 1]
+    cw, tree, root = oracle.commit(packed, r0, k, kind, n_threads=8)
+    ot = OT()
+    ot.absorb_slice(b"outer protocol")
+    exp = oprove(OZ(ot), OCfg(k, ks, rates, qs, gb, fb, ood, kind), packed, basis, target, cw,
+                 tree, root)
+    c, pd = commit(packed, PcsParams(lm + 7, r0, k, kind), ctx)
+    dp, db = DeviceArray.from_host(packed, ctx), DeviceArray.from_host(basis, ctx)
+    t = Blake3Transcript()
+    t.absorb_slice(b"outer protocol")
+    try:
+        got = prove(t, pd, dp, db, target, LigeritoConfig(k, ks, rates, qs, gb, fb, ood, kind),
+                    ctx)
+        blob = codec.encode_ligerito(got)
+        assert blob == OC.encode_ligerito(exp)
+        assert t.state_digest() == ot.state_digest()
+        return blob
+    finally:
+        pd.free()
+        dp.free()
+        db.free()
+
+
+@pytest.mark.parametrize("case", PROVE_CASES)
+def test_prove_matches_oracle(oracle, ctx, case):
+    _prove_both(oracle, ctx, case, seed=case[0] + 1)
+
+
+def test_prove_rejects_bad_config(oracle, ctx):
+    from bitz_gb300 import (Blake3Transcript, BzError, DeviceArray, LigeritoConfig, PcsParams,
+                            commit, prove)
+
+    lm, r0, k = 10, 2, 4
+    packed = oracle.chacha_words(1, 1 << lm)
+    c, pd = commit(packed, PcsParams(lm + 7, r0, k, 1), ctx)
+    dp = DeviceArray.from_host(packed, ctx)
+    bad = [
+        LigeritoConfig(k, [2], [1, 1], [4, 4], [0, 0]),                  # rate 0 != commitment
+        LigeritoConfig(k, [7], [2, 1], [4, 4], [0, 0]),                  # k exceeds folded length
+        LigeritoConfig(k, [2], [2, 1], [4, 4], [0, 0], ood_samples=[1, 0]),  # OOD at level 0
+        LigeritoConfig(k, [2], [2, 1], [4, 1000], [0, 0]),               # queries > block length
+        LigeritoConfig(k + 1, [2], [2, 1], [4, 4], [0, 0]),              # initial_k != lanes
+    ]
+    try:
+        for cfg in bad:
+            with pytest.raises(BzError):
+                prove(Blake3Transcript(), pd, dp, dp, [0, 0], cfg, ctx)
+        with pytest.raises(ValueError):
+            LigeritoConfig(k, [2], [2], [4, 4], [0, 0]).to_c()
+    finally:
+        pd.free()
+        dp.free()
+
+
+def test_prove_c2_shape(oracle, ctx):
+    """The 2^24-element witness (2^12 lanes x 2^12 columns, rate 1/4) with a
+    two-step recursion: the benchmark's full opening shape."""
+    _prove_both(oracle, ctx, (24, 2, 12, [6, 3], [2, 2, 2], [148, 100, 60], [16, 10, 8],
+                              [4, 2, 0], None, 1), seed=1)

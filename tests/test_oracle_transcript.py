@@ -172,3 +172,51 @@ def test_oracle_l0_opening_consistency(oracle):
     assert res.alpha.shape == (4, 2)
     _, _, root1 = oracle.commit(res.folded, 2, 3, oracle.BLAKE3)
     assert root1 == res.root1
+
+
+def test_oracle_full_prover_consistency(oracle):
+    """The oracle's recursive Ligerito proof: every level's rows authenticate
+    against that level's root, the final rows against the last root, the
+    proof has the reference's per-level counts, and its bincode blob round
+    trips."""
+    from oracle import codec as OC
+    from oracle.ligerito import LigeritoConfig, prove
+    from oracle.transcript import Blake3Transcript, ZincChallenger
+
+    lm, r0, k = 12, 2, 4
+    packed = oracle.chacha_words(21, 1 << lm)
+    basis = oracle.chacha_words(22, 1 << lm)
+    cw, tree, root = oracle.commit(packed, r0, k, oracle.BLAKE3)
+    cfg = LigeritoConfig(initial_k=k, recursive_ks=[3, 2], log_inv_rates=[r0, 2, 1],
+                         queries=[10, 6, 5], grinding_bits=[4, 3, 2],
+                         fold_grinding_bits=[3, 2, 0], ood_samples=[0, 1, 2])
+    p = prove(ZincChallenger(Blake3Transcript()), cfg, packed, basis, [5, 6], cw, tree, root)
+    assert len(p.recursive_roots) == 2 and len(p.recursive_proofs) == 1
+    assert len(p.grinding_nonces) == 3 and len(p.ood_values) == 3
+    # messages: 1 + initial_k folds + OOD intros + one intro per induced basis
+    # (level 0 and each non-final level) + the recursive folds
+    assert len(p.sumcheck_transcript) == 1 + k + 3 + 2 + 3 + 2
+    # fold grinds: 3,2,1 bits at level 0 (j < 3), 2,1 bits at level 1
+    assert len(p.fold_grinding_nonces) == 3 + 2
+    assert len(p.final_proof.yr) == 1 << (lm - k - 3 - 2)
+
+    trace = {}
+    p_t = prove(ZincChallenger(Blake3Transcript()), cfg, packed, basis, [5, 6], cw, tree, root,
+                trace=trace)
+    opened = [p_t.initial_proof, *p_t.recursive_proofs, p_t.final_proof]
+    assert [lv[0] for lv in trace["levels"]] == [root, *p_t.recursive_roots]
+    for (lroot, block_len, qs), lev in zip(trace["levels"], opened):
+        lh = np.array([np.frombuffer(oracle.hash_leaf(
+            np.array(r, dtype=np.uint64).astype("<u8").tobytes(), oracle.BLAKE3), np.uint8)
+            for r in lev.opened_rows])
+        pr = np.frombuffer(b"".join(lev.merkle_proof), np.uint8).reshape(-1, 32)
+        assert oracle.verify_merkle_multi_proof(lroot, block_len, qs, lh, pr, oracle.BLAKE3)
+    # the transcript replays: rebuild queries from a second run's challenger
+    p2 = prove(ZincChallenger(Blake3Transcript()), cfg, packed, basis, [5, 6], cw, tree, root)
+    assert OC.encode_ligerito(p) == OC.encode_ligerito(p2)
+    blob = OC.encode_ligerito(p)
+    assert OC.encode_ligerito(OC.decode_ligerito(blob)) == blob
+    assert len(p.initial_proof.opened_rows) == 10
+    assert all(len(r) == 1 << k for r in p.initial_proof.opened_rows)
+    assert all(len(r) == 1 << 3 for r in p.recursive_proofs[0].opened_rows)
+    assert all(len(r) == 1 << 2 for r in p.final_proof.opened_rows)
