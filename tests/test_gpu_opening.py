@@ -192,7 +192,7 @@ PROVE_CASES = [
     (10, 1, 2, [2], [1, 1], [4, 3], [0, 0], None, None, 1),
     (12, 2, 4, [3, 2], [2, 2, 1], [10, 6, 5], [4, 3, 2], [3, 2, 0], [0, 1, 2], 1),
     (12, 2, 6, [2], [2, 2], [40, 12], [0, 6], [8, 0], [0, 1], 0),
-    (14, 2, 7, [3, 2], [2, 2, 2], [64, 30, 20], [8, 6, 4], None, [0, 0, 1], 1),
+    (14, 2, 7, [3, 2], [2, 2, 2], [64, 30, 12], [8, 6, 4], None, [0, 0, 1], 1),
     (16, 2, 8, [4], [2, 2], [148, 60], [12, 10], [10, 6], None, 1),
 ]
 
@@ -264,5 +264,5 @@ def test_prove_rejects_bad_config(oracle, ctx):
 def test_prove_c2_shape(oracle, ctx):
     """The 2^24-element witness (2^12 lanes x 2^12 columns, rate 1/4) with a
     two-step recursion: the benchmark's full opening shape."""
-    _prove_both(oracle, ctx, (24, 2, 12, [6, 3], [2, 2, 2], [148, 100, 60], [16, 10, 8],
+    _prove_both(oracle, ctx, (24, 2, 12, [6, 3], [2, 2, 2], [148, 100, 30], [16, 10, 8],
                               [4, 2, 0], None, 1), seed=1)
