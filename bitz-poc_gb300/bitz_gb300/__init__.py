@@ -24,3 +24,4 @@ from .pcs import (  # noqa: F401
 from .transcript import Blake3Transcript, ZincChallenger, blake3_xof, pow_first_nonce  # noqa: F401,E402
 from .opening import L0Config, L0Opening, LigeritoConfig, open_l0, prove  # noqa: F401,E402
 from . import codec  # noqa: F401,E402
+from .binary_pcs import BinaryPcs, BitMleOpening, Round0Prover  # noqa: F401,E402

@@ -99,6 +99,14 @@ _SIGS = {
     "bz_l0_opening_free": (_I, [_P]),
     "bz_l0_opening_ood_values": (_I, [_P, _P]),
     "bz_ligerito_prove": (_I, [_P, _P, _P, _P, _P, _P, _P, _PP]),
+    "bz_pcs_prove_round0": (_I, [_P, _P, _P, _S, _U32, _PP]),
+    "bz_round0_get": (_I, [_P, _P, ctypes.POINTER(_I), ctypes.POINTER(_U64),
+                           ctypes.POINTER(_U32)]),
+    "bz_round0_point": (_I, [_P, _P]),
+    "bz_round0_free": (_I, [_P]),
+    "bz_pcs_ring_switch": (_I, [_P, _P, _P, _S, _P, _P, _P, _P]),
+    "bz_pcs_open_basis": (_I, [_P, _P, _P, _P, _P, _P, _P, _P, _PP]),
+    "bz_pcs_open_bit_mle": (_I, [_P, _P, _P, _P, _P, _P, _S, _P, _P, _PP]),
     "bz_ligerito_proof_encode": (_I, [_P, _P, _S, ctypes.POINTER(_S)]),
     "bz_ligerito_proof_decode": (_I, [_P, _S, _PP]),
     "bz_ligerito_proof_view_of": (_I, [_P, _P]),

@@ -137,6 +137,15 @@ int launch_glue(uint4 *d_b, const uint4 *d_nb, size_t n, uint4 beta, cudaStream_
 size_t dot_partials_count(size_t n, int num_sms);
 int launch_dot(const uint4 *d_f, const uint4 *d_b, size_t n, uint4 *d_partial, uint4 *d_out,
                cudaStream_t st, int num_sms);
+// d_out[0] = sum_h head[h] * sum_j p[h 2^lo + j] * tail[j] over n_blocks blocks;
+// d_partial holds split_dot_partials(n_blocks) elements.
+size_t split_dot_partials(size_t n_blocks, int num_sms);
+int launch_split_dot(const uint4 *d_p, const uint4 *d_tail, int lo, const uint4 *d_head,
+                     size_t n_blocks, uint4 *d_partial, uint4 *d_out, cudaStream_t st,
+                     int num_sms);
+// d_b[i] += eta * head[i >> lo] * tail[i mod 2^lo]
+int launch_eq_axpy(uint4 *d_b, const uint4 *d_tail, int lo, const uint4 *d_head, uint4 eta,
+                   size_t n, cudaStream_t st);
 
 // One-time kernel attributes (large dynamic shared memory), called when a
 // context is created so no attribute call happens during graph capture.

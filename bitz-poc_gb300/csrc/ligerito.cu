@@ -10,6 +10,10 @@
 //    :3125-3145).
 //  * dot: sum_j f[j] * b[j], the claimed value of an out-of-domain
 //    introduce (round_msg_and_eval_lsb, :2550-2587).
+//  * the BitZ round-0 out-of-domain sample over the packed message: its
+//    value MLE[P](point) and the eta * eq(point) term added to the opening
+//    basis, both with eq(point) split into a 2^12-entry low table and a high
+//    table (src/ligerito_flock.rs:1456-1486, 1590-1650).
 //
 // These arrays are the folded witness (2^(n - initial_k) elements and less),
 // so the kernels are simple one-pass forms; sums are XORs of reduced
@@ -100,9 +104,59 @@ __global__ void __launch_bounds__(kThreads) dot_kernel(const uint4 *f, const uin
     if (threadIdx.x == 0) partial[blockIdx.x] = acc;
 }
 
+// The out-of-domain MLE split at 2^lo-element blocks (ood_eval,
+// src/ligerito_flock.rs:1456-1486): CTA h computes
+// head[h] * sum_j p[h * 2^lo + j] * tail[j] for its blocks h = blockIdx.x +
+// k * gridDim.x and writes one partial.
+__global__ void __launch_bounds__(kThreads) split_dot_kernel(const uint4 *p, const uint4 *tail,
+                                                             int lo, const uint4 *head,
+                                                             uint64_t n_blocks, uint4 *partial) {
+    const uint64_t bl = (uint64_t)1 << lo;
+    uint4 acc = make_uint4(0, 0, 0, 0);
+    for (uint64_t h = blockIdx.x; h < n_blocks; h += gridDim.x) {
+        uint4 inner = make_uint4(0, 0, 0, 0);
+        for (uint64_t j = threadIdx.x; j < bl; j += blockDim.x)
+            inner = gf_add(inner, gf_mul(p[h * bl + j], tail[j]));
+        acc = gf_add(acc, gf_mul(inner, head[h]));
+    }
+    acc = cta_xor_u4(acc);
+    if (threadIdx.x == 0) partial[blockIdx.x] = acc;
+}
+
+// b[i] += (eta * head[i >> lo]) * tail[i & (2^lo - 1)]  (add_ood_basis,
+// src/ligerito_flock.rs:1590-1650: eta * eq(point) added to the basis)
+__global__ void eq_axpy_kernel(uint4 *b, const uint4 *tail, int lo, const uint4 *head, uint4 eta,
+                               uint64_t n) {
+    const uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const uint4 s = gf_mul(eta, head[i >> lo]);
+    b[i] = gf_add(b[i], gf_mul(s, tail[i & (((uint64_t)1 << lo) - 1)]));
+}
+
 unsigned grid_for(uint64_t n) { return (unsigned)((n + kThreads - 1) / kThreads); }
 
 }  // namespace
+
+size_t split_dot_partials(size_t n_blocks, int num_sms) {
+    const size_t cap = (size_t)num_sms * 4;
+    return n_blocks < cap ? (n_blocks ? n_blocks : 1) : cap;
+}
+
+int launch_split_dot(const uint4 *d_p, const uint4 *d_tail, int lo, const uint4 *d_head,
+                     size_t n_blocks, uint4 *d_partial, uint4 *d_out, cudaStream_t st,
+                     int num_sms) {
+    const size_t ctas = split_dot_partials(n_blocks, num_sms);
+    split_dot_kernel<<<(unsigned)ctas, kThreads, 0, st>>>(d_p, d_tail, lo, d_head, n_blocks,
+                                                          d_partial);
+    xor_reduce_kernel<<<1, kThreads, 0, st>>>(d_partial, ctas, d_out);
+    return 2;
+}
+
+int launch_eq_axpy(uint4 *d_b, const uint4 *d_tail, int lo, const uint4 *d_head, uint4 eta,
+                   size_t n, cudaStream_t st) {
+    eq_axpy_kernel<<<grid_for(n), kThreads, 0, st>>>(d_b, d_tail, lo, d_head, eta, n);
+    return 1;
+}
 
 int launch_induce_basis(uint4 *d_domain, int log_d, const uint64_t *d_pos, const uint4 *d_w,
                         int nq, const uint4 *d_tw, cudaStream_t st) {

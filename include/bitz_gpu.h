@@ -476,6 +476,42 @@ int bz_read_ring_switch(bz_reader *r, uint64_t s_v[256]);
  * 64 MiB or the bytes left; BZ_ERR_DECODE when the blob does not decode. */
 int bz_read_ligerito(bz_reader *r, bz_ligerito_proof **out);
 
+/* ---- BitZ BinaryPcs opening ------------------------------------------------ */
+/* Round 0, the out-of-domain sample bound right after the commitment
+ * (BinaryPcs::prove_round0, src/binary_pcs.rs:320-325;
+ * prove_ood_round_packed, src/ligerito_flock.rs:1520-1557): header frame,
+ * grinding when grinding_bits > 0, zeta, y = MLE[packed](zeta, zeta^2, ...)
+ * on the device, y absorbed.  d_packed holds n = 2^vars elements. */
+typedef struct bz_round0 bz_round0;
+int bz_pcs_prove_round0(bz_ctx *ctx, bz_transcript *transcript, const uint64_t *d_packed,
+                        size_t n, uint32_t grinding_bits, bz_round0 **out);
+/* OodRound {y, nonce}: has_nonce = 1 iff grinding_bits > 0; vars = log2 n. */
+int bz_round0_get(const bz_round0 *r, uint64_t y[2], int *has_nonce, uint64_t *nonce,
+                  uint32_t *vars);
+/* The point (zeta^(2^i)), vars x 2 words. */
+int bz_round0_point(const bz_round0 *r, uint64_t *point);
+int bz_round0_free(bz_round0 *r);
+/* ring_switch_prove (src/ligerito.rs:445-496): r_hi has log2 n coordinates;
+ * s_v receives the 128 partial evaluations (absorbed), d_basis (n elements,
+ * device) the weight table B(y), target beta0. */
+int bz_pcs_ring_switch(bz_ctx *ctx, bz_transcript *transcript, const uint64_t *d_packed, size_t n,
+                       const uint64_t *r_hi, uint64_t s_v[256], uint64_t *d_basis,
+                       uint64_t target[2]);
+/* BinaryPcs::open_basis (src/binary_pcs.rs:341-367): eta, d_basis +=
+ * eta * eq(round-0 point) in place, target + eta * y, then bz_ligerito_prove. */
+int bz_pcs_open_basis(bz_ctx *ctx, bz_transcript *transcript, bz_commitment *c0,
+                      const uint64_t *d_packed, const bz_round0 *round0, uint64_t *d_basis,
+                      const uint64_t target[2], const bz_ligerito_config *cfg,
+                      bz_ligerito_proof **out);
+/* BinaryPcs::open_bit_mle (src/binary_pcs.rs:413-431): point has
+ * point_len = log_msg_len + 7 coordinates (the low 7 select the bit of a
+ * word); ring switch on point[7..], then open_basis.  The BitMleOpening is
+ * (s_v, *out). */
+int bz_pcs_open_bit_mle(bz_ctx *ctx, bz_transcript *transcript, bz_commitment *c0,
+                        const uint64_t *d_packed, const bz_round0 *round0, const uint64_t *point,
+                        size_t point_len, const bz_ligerito_config *cfg, uint64_t s_v[256],
+                        bz_ligerito_proof **out);
+
 /* ---- synthetic inputs --------------------------------------------------- */
 /* RFC 8439 ChaCha20 keystream words (key = seed LE u64 zero padded, nonce 0,
  * counter from 0), word i = keystream bytes [16 i, 16 i + 16). */

@@ -220,3 +220,87 @@ def test_oracle_full_prover_consistency(oracle):
     assert all(len(r) == 1 << k for r in p.initial_proof.opened_rows)
     assert all(len(r) == 1 << 3 for r in p.recursive_proofs[0].opened_rows)
     assert all(len(r) == 1 << 2 for r in p.final_proof.opened_rows)
+
+
+def _bit_mle(packed, point):
+    """MLE over the bits of the packed words at point (low 7 coordinates pick
+    the bit of a word), by its definition."""
+    from oracle import oracle as O
+
+    eq_lo = O.build_eq_lsb(point[:7])
+    eq_hi = O.build_eq_lsb(point[7:])
+    bits = np.unpackbits(np.ascontiguousarray(packed, "<u8").view(np.uint8).reshape(-1, 16),
+                         axis=1, bitorder="little")                     # [y, v]
+    acc = np.zeros(2, np.uint64)
+    for y in range(packed.shape[0]):
+        sel = eq_lo[bits[y].astype(bool)]
+        if sel.shape[0]:
+            acc ^= O.gf_mul(np.bitwise_xor.reduce(sel, axis=0), eq_hi[y])
+    return acc
+
+
+def test_oracle_ring_switch_identities(oracle):
+    """ring_switch_prove's debug identity (src/ligerito.rs:478-487):
+    sum_y B(y) * P(y) = beta0, and the verifier's claim check (:510-516):
+    sum_v eq(r_lo, v) * s_v = the bit-MLE value at the full point."""
+    from oracle.binary_pcs import ring_switch_prove
+    from oracle.transcript import Blake3Transcript
+
+    rng = np.random.default_rng(3)
+    m = 8
+    packed = rng.integers(0, 2**64, (1 << m, 2), dtype=np.uint64)
+    point = rng.integers(0, 2**64, (m + 7, 2), dtype=np.uint64)
+    s, b, beta0 = ring_switch_prove(Blake3Transcript(), packed, point[7:])
+    assert (np.bitwise_xor.reduce(oracle.gf_mul_many(b, packed), axis=0) == beta0).all()
+    eq_lo = oracle.build_eq_lsb(point[:7])
+    mu = np.bitwise_xor.reduce(oracle.gf_mul_many(s, eq_lo), axis=0)
+    assert (mu == _bit_mle(packed, point)).all()
+
+
+def test_oracle_round0_and_ood_basis(oracle):
+    """ood_eval (split at 2^12-element blocks) equals <P, eq(point)> over the
+    full eq table; round 0 grinds, draws and absorbs deterministically."""
+    from oracle.binary_pcs import ood_eval, ood_point, prove_round0
+    from oracle.transcript import Blake3Transcript
+
+    rng = np.random.default_rng(4)
+    for m in (0, 3, 12, 14):
+        packed = rng.integers(0, 2**64, (1 << m, 2), dtype=np.uint64)
+        pt = ood_point(rng.integers(0, 2**64, 2, dtype=np.uint64), m)
+        full = oracle.build_eq_lsb(pt)
+        expect = np.bitwise_xor.reduce(oracle.gf_mul_many(packed, full), axis=0)
+        assert (ood_eval(packed, pt) == expect).all()
+        if m:
+            assert (pt[1] == oracle.gf_mul(pt[0], pt[0])).all()
+    packed = rng.integers(0, 2**64, (1 << 10, 2), dtype=np.uint64)
+    a, b = Blake3Transcript(), Blake3Transcript()
+    ra, rb = prove_round0(a, packed, 6), prove_round0(b, packed, 6)
+    assert ra.nonce == rb.nonce and ra.nonce is not None
+    assert a.state_digest() == b.state_digest() and (ra.y == rb.y).all()
+    assert prove_round0(Blake3Transcript(), packed, 0).nonce is None
+
+
+def test_oracle_open_bit_mle_runs(oracle):
+    from oracle import codec as OC
+    from oracle.binary_pcs import open_bit_mle, prove_round0
+    from oracle.ligerito import LigeritoConfig
+    from oracle.transcript import Blake3Transcript
+
+    m, k = 10, 5
+    packed = oracle.chacha_words(8, 1 << m)
+    cw, tree, root = oracle.commit(packed, 2, k, oracle.BLAKE3)
+    t = Blake3Transcript()
+    t.absorb_slice(root)
+    r0 = prove_round0(t, packed, 4)
+    point = np.random.default_rng(5).integers(0, 2**64, (m + 7, 2), dtype=np.uint64)
+    cfg = LigeritoConfig(k, [3], [2, 2], [20, 10], [4, 2], [2, 1], [0, 1])
+    s_v, lig = open_bit_mle(t, cfg, packed, cw, tree, root, r0, point)
+    w = OC.Writer()
+    w.round0(r0.y, r0.nonce)
+    w.ring_switch(s_v)
+    w.ligerito(lig)
+    r = OC.Reader(bytes(w.buf))
+    y, nonce = r.round0()
+    assert list(y) == list(r0.y) and nonce == r0.nonce
+    assert [tuple(g) for g in r.ring_switch()] == [tuple(int(x) for x in g) for g in s_v]
+    assert OC.encode_ligerito(r.ligerito()) == OC.encode_ligerito(lig)
