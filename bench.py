@@ -174,7 +174,20 @@ def cpu_baseline(n_threads: int, log_n: int = LOG_N):
     prove(ZincChallenger(t), LigeritoConfig(**open_config(LOG_LANES)), msg, basis, [1, 2], cw,
           tree, root)
     open_ms = (time.perf_counter() - t1) * 1e3
-    return (1 << log_n) / dt, dt, root, open_ms
+    # the 2^20-word bit-MLE opening (round 0 + open_bit_mle), as the GPU leg
+    from oracle.binary_pcs import open_bit_mle, prove_round0
+
+    m = 20
+    p20 = O.chacha_words(0, 1 << m)
+    cw20, tree20, root20 = O.commit(p20, 2, 10, HASH, n_threads=n_threads)
+    point = np.random.default_rng(0).integers(0, 2**64, (m + 7, 2), dtype=np.uint64)
+    t2 = Blake3Transcript()
+    t2.absorb_slice(root20)
+    t3 = time.perf_counter()
+    r0 = prove_round0(t2, p20, BIT_MLE_ROUND0_BITS)
+    open_bit_mle(t2, LigeritoConfig(**BIT_MLE_CONFIG), p20, cw20, tree20, root20, r0, point)
+    bit_mle_ms = (time.perf_counter() - t3) * 1e3
+    return (1 << log_n) / dt, dt, root, open_ms, bit_mle_ms
 
 
 def run_reference(args, ws, rank):
@@ -270,11 +283,14 @@ def run_gpu(args, ws, rank, local):
     total_ms = D.max(total_ms)
     value = ws * args.steps * (1 << LOG_N) / (total_ms / 1e3)
 
-    if args.only_commit:
+    if args.only_commit or args.only_open:
         if rank == 0:
-            print(json.dumps({"metric": METRIC, "value": value, "unit": UNIT, "log_n": LOG_N,
-                              "ms_per_step": total_ms / args.steps, "schedule": schedule,
-                              "root": root0.hex()}), flush=True)
+            line = {"metric": METRIC, "value": value, "unit": UNIT, "log_n": LOG_N,
+                    "ms_per_step": total_ms / args.steps, "schedule": schedule,
+                    "root": root0.hex()}
+            if args.only_open:
+                line["opening"] = _bench_open(ctx, bz, msg, params)
+            print(json.dumps(line), flush=True)
         msg.free()
         ctx.close()
         D.close()
@@ -372,12 +388,12 @@ def run_gpu(args, ws, rank, local):
         cpu = None
         if not args.skip_cpu:
             threads = os.cpu_count() or 1
-            v, dt, croot, cpu_open_ms = cpu_baseline(threads)
+            v, dt, croot, cpu_open_ms, cpu_bit_mle_ms = cpu_baseline(threads)
             assert croot == root0 or rank != 0 or SEED + rank != SEED
             cpu = {"value": v, "unit": UNIT, "cores": threads, "kind": "port",
                    "sample": f"one full 2^24-element commit ({dt:.2f} s) by the CPU "
                              "restatement of the reference on all host threads",
-                   "prove_ms": cpu_open_ms}
+                   "prove_ms": cpu_open_ms, "bit_mle_2^20_round0_and_open_ms": cpu_bit_mle_ms}
         sorted_ms = sorted(step_ms)
         p99 = sorted_ms[min(len(sorted_ms) - 1, int(round(0.99 * (len(sorted_ms) - 1))))]
         out = {
@@ -552,7 +568,52 @@ def _bench_open(ctx, bz, msg, params):
     info["pow_24bit_hashes_per_s_lower_bound"] = float(np.median(pw))
     pd.free()
     b.free()
+    info["bit_mle_2^20"] = _bench_bit_mle(ctx, bz)
     return info
+
+
+BIT_MLE_CONFIG = dict(initial_k=10, recursive_ks=[5], log_inv_rates=[2, 2], queries=[148, 64],
+                      grinding_bits=[16, 8], fold_grinding_bits=[0, 2], ood_samples=[0, 1],
+                      hash_kind=1)
+BIT_MLE_ROUND0_BITS = 8
+
+
+def _bench_bit_mle(ctx, bz):
+    """The 2^20-word witness (2^10 lanes x 2^10 columns, rate 1/4, ChaCha seed
+    0) opened at one random point through BinaryPcs: commit, round 0 (8-bit
+    grind), open_bit_mle (ring switch + open_basis + recursive Ligerito,
+    BIT_MLE_CONFIG).  Host wall time per call, median of 3 after a warm-up."""
+    from bitz_gb300 import codec
+
+    m = 20
+    pcs = bz.BinaryPcs(m, bz.LigeritoConfig(**BIT_MLE_CONFIG), BIT_MLE_ROUND0_BITS, ctx)
+    d = bz.DeviceArray.chacha(0, 1 << m, ctx)
+    point = np.random.default_rng(0).integers(0, 2**64, (m + 7, 2), dtype=np.uint64)
+    ts = {"commit_ms": [], "round0_ms": [], "open_bit_mle_ms": []}
+    nbytes = 0
+    for _ in range(4):
+        ctx.synchronize()
+        t0 = time.perf_counter()
+        c, pd = pcs.commit(d)
+        t = bz.Blake3Transcript()
+        t.absorb_slice(c.root)
+        t1 = time.perf_counter()
+        r0 = pcs.prove_round0(t, d)
+        t2 = time.perf_counter()
+        op = pcs.open_bit_mle(t, d, pd, r0, point)
+        t3 = time.perf_counter()
+        w = codec.Writer()
+        r0.write(w)
+        op.write(w)
+        nbytes = len(w.into_bytes())
+        pd.free()
+        for k, v in zip(ts, (t1 - t0, t2 - t1, t3 - t2)):
+            ts[k].append(v * 1e3)
+    d.free()
+    out = {k: statistics.median(v[1:]) for k, v in ts.items()}
+    out["proof_stream_bytes"] = nbytes
+    out["config"] = "BinaryPcs round 0 (8-bit grind) + open_bit_mle, " + str(BIT_MLE_CONFIG)
+    return out
 
 
 def _geometric_sizes(rng, n, lo=14, hi=26, q=0.97):
@@ -646,6 +707,8 @@ def main():
     ap.add_argument("--no-autotune", action="store_true")
     ap.add_argument("--only-commit", action="store_true",
                     help="time the device commit loop only (profiling runs)")
+    ap.add_argument("--only-open", action="store_true",
+                    help="the device commit loop and the opening leg only (profiling runs)")
     ap.add_argument("--log-n", type=int, default=None, help="override log2 elements")
     ap.add_argument("--serve-requests", type=int, default=160)
     args = ap.parse_args()
