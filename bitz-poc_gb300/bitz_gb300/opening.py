@@ -64,6 +64,7 @@ class L0Opening:
     def __init__(self, handle, ctx: Context):
         self.handle = handle
         self.ctx = ctx
+        ctx.adopt(self)
         sz = L0SizesC()
         check(ctx.handle, lib().bz_l0_opening_sizes(handle, ctypes.byref(sz)))
         self.sizes = sz
@@ -110,8 +111,11 @@ class L0Opening:
 
     def free(self):
         if self.handle:
-            lib().bz_l0_opening_free(self.handle)
+            if self.ctx.handle:
+                lib().bz_l0_opening_free(self.handle)
             self.handle = None
+
+    release = free
 
     def __del__(self):
         try:

@@ -11,8 +11,10 @@ reference ``assert!``s raise ``ValueError`` here; device failures raise
 """
 from __future__ import annotations
 
+import atexit
 import ctypes
 import threading
+import weakref
 from dataclasses import dataclass
 
 import numpy as np
@@ -73,8 +75,17 @@ class PcsParams:
         return Params(self.log_msg_len(), self.log_inv_rate, self.log_batch_size, self.merkle_hash)
 
 
+_contexts: "weakref.WeakSet[Context]" = weakref.WeakSet()
+
+
 class Context:
-    """One device context (stream, memory budget, twiddle and schedule caches)."""
+    """One device context (stream, memory budget, twiddle and schedule caches).
+
+    Objects that hold device resources of this context (device arrays,
+    commitments, openings, batch plans, servers) register with it; ``close``
+    releases them first, then the context, and every open context is closed
+    at interpreter exit, so teardown order never depends on the garbage
+    collector."""
 
     def __init__(self, device: int = 0, mem_budget_bytes: int = 0):
         L = lib()
@@ -82,9 +93,21 @@ class Context:
         check(None, L.bz_ctx_create(device, mem_budget_bytes, ctypes.byref(h)))
         self.handle = h
         self.device = device
+        self._children = weakref.WeakSet()
+        _contexts.add(self)
+
+    def adopt(self, obj):
+        """Register obj (with a ``release()`` method) for release before close."""
+        self._children.add(obj)
+        return obj
 
     def close(self):
         if self.handle:
+            for ch in list(self._children):
+                try:
+                    ch.release()
+                except Exception:
+                    pass
             lib().bz_ctx_destroy(self.handle)
             self.handle = None
 
@@ -154,6 +177,12 @@ _default = None
 _default_lock = threading.Lock()
 
 
+@atexit.register
+def _close_contexts():
+    for c in list(_contexts):
+        c.close()
+
+
 def default_context() -> Context:
     global _default
     with _default_lock:
@@ -172,6 +201,7 @@ class DeviceArray:
         check(self.ctx.handle, lib().bz_device_alloc(self.ctx.handle, max(self.n, 1) * 16,
                                                      ctypes.byref(p)))
         self.ptr = p
+        self.ctx.adopt(self)
 
     @classmethod
     def from_host(cls, a: np.ndarray, ctx: Context | None = None) -> "DeviceArray":
@@ -193,8 +223,11 @@ class DeviceArray:
 
     def free(self):
         if self.ptr:
-            lib().bz_device_free(self.ctx.handle, self.ptr)
+            if self.ctx.handle:  # a closed context already released its memory
+                lib().bz_device_free(self.ctx.handle, self.ptr)
             self.ptr = None
+
+    release = free
 
     def __del__(self):
         try:
@@ -218,6 +251,7 @@ class ProverData:
         self.handle = handle
         self.params = params
         self.ctx = ctx
+        ctx.adopt(self)
 
     def _h(self):
         if not self.handle:
@@ -267,8 +301,11 @@ class ProverData:
 
     def free(self):
         if self.handle:
-            lib().bz_commitment_free(self.handle)
+            if self.ctx.handle:  # a closed context already freed its commitments
+                lib().bz_commitment_free(self.handle)
             self.handle = None
+
+    release = free
 
     def __del__(self):
         try:
@@ -393,6 +430,7 @@ class BatchPlan:
                                                       1 if use_graph else 0, n_branches,
                                                       ctypes.byref(h)))
         self.h = h
+        self.ctx.adopt(self)
 
     def launch(self):
         check(self.ctx.handle, self.L.bz_batch_plan_launch(self.h))
@@ -411,8 +449,11 @@ class BatchPlan:
 
     def close(self):
         if self.h:
-            self.L.bz_batch_plan_destroy(self.h)
+            if self.ctx.handle:
+                self.L.bz_batch_plan_destroy(self.h)
             self.h = None
+
+    release = close
 
     def __del__(self):
         try:

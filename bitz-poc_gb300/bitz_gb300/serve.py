@@ -56,11 +56,15 @@ class Server:
                                                        queue_cap, ctypes.byref(h)))
         self.h = h
         self._keep = {}  # request id -> host buffer kept alive until committed
+        self.ctx.adopt(self)
 
     def close(self):
         if self.h:
-            self.L.bz_server_destroy(self.h)
+            if self.ctx.handle:
+                self.L.bz_server_destroy(self.h)
             self.h = None
+
+    release = close
 
     def __enter__(self):
         return self

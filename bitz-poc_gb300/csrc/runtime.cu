@@ -181,6 +181,12 @@ uint32_t schedule_for(bz_ctx *ctx, const Shape &s) {
     return default_schedule(s);
 }
 
+// Every live commitment of every context: bz_commitment_free checks a handle
+// here before touching it, so a handle whose context was destroyed (which
+// frees the context's commitments) is refused instead of used after free.
+static std::mutex g_handles_mu;
+static std::set<const bz_commitment *> g_handles;
+
 // Allocate a commitment's resident buffers (budgeted).
 int alloc_commitment(bz_ctx *ctx, const Shape &s, bz_commitment **out) {
     bz_commitment *c = new bz_commitment();
@@ -202,6 +208,10 @@ int alloc_commitment(bz_ctx *ctx, const Shape &s, bz_commitment **out) {
     {
         std::lock_guard<std::mutex> g(ctx->live_mu);
         ctx->live.insert(c);
+    }
+    {
+        std::lock_guard<std::mutex> g(g_handles_mu);
+        g_handles.insert(c);
     }
     *out = c;
     return BZ_OK;
@@ -676,6 +686,10 @@ int bz_commitment_multiproof(bz_commitment *c, const uint64_t *positions, size_t
 
 int bz_commitment_free(bz_commitment *c) {
     if (!c) return BZ_ERR_ARG;
+    {
+        std::lock_guard<std::mutex> g(g_handles_mu);
+        if (!g_handles.erase(c)) return BZ_ERR_STATE;  // freed, or its context destroyed
+    }
     bz_ctx *ctx = c->ctx;
     {
         std::lock_guard<std::mutex> g(ctx->live_mu);
