@@ -108,12 +108,25 @@ __global__ void __launch_bounds__(256) round_msg_kernel(const uint4 *f, const ui
 }
 
 // Final XOR of per-CTA partials and the single reduction: out = {u0, u2}.
-__global__ void finish_msg_kernel(const uint64_t *partials, int n, uint64_t *out) {
+// 256 threads: thread t XORs word t mod 8 of partials t / 8, t / 8 + 32, ...;
+// lanes holding the same word then combine by shuffles and across warps.
+constexpr int kFinishThreads = 256;
+__global__ void __launch_bounds__(kFinishThreads) finish_msg_kernel(const uint64_t *partials,
+                                                                    int n, uint64_t *out) {
+    __shared__ uint64_t red[kFinishThreads / 32][8];
     __shared__ uint64_t acc[8];
+    const int w = threadIdx.x & 7;
+    uint64_t a = 0;
+    for (int i = threadIdx.x >> 3; i < n; i += kFinishThreads / 8)
+        a ^= partials[(uint64_t)i * 8 + w];
+    a ^= __shfl_xor_sync(0xffffffffu, a, 8);
+    a ^= __shfl_xor_sync(0xffffffffu, a, 16);
+    if ((threadIdx.x & 31) < 8) red[threadIdx.x >> 5][w] = a;
+    __syncthreads();
     if (threadIdx.x < 8) {
-        uint64_t a = 0;
-        for (int i = 0; i < n; ++i) a ^= partials[(uint64_t)i * 8 + threadIdx.x];
-        acc[threadIdx.x] = a;
+        uint64_t x = 0;
+        for (int k = 0; k < kFinishThreads / 32; ++k) x ^= red[k][threadIdx.x];
+        acc[threadIdx.x] = x;
     }
     __syncthreads();
     if (threadIdx.x == 0) {
@@ -147,7 +160,7 @@ int launch_fold_and_msg(const uint4 *d_f, const uint4 *d_b, size_t n, uint4 r, u
     const int grid = std::min(msg_grid(half / 2, num_sms), 1024);
     fold_and_msg_kernel<<<grid, 256, kRTableSmem, st>>>(d_f, d_b, half, r, d_nf, d_nb,
                                                          d_partials);
-    finish_msg_kernel<<<1, 32, 0, st>>>(d_partials, grid, d_msg_out);
+    finish_msg_kernel<<<1, kFinishThreads, 0, st>>>(d_partials, grid, d_msg_out);
     return 2;
 }
 
@@ -156,7 +169,7 @@ int launch_round_msg(const uint4 *d_f, const uint4 *d_b, size_t n, uint64_t *d_p
     const uint64_t pairs = n / 2;
     const int grid = std::min(msg_grid(pairs, num_sms), 1024);
     round_msg_kernel<<<grid, 256, 0, st>>>(d_f, d_b, pairs, d_partials);
-    finish_msg_kernel<<<1, 32, 0, st>>>(d_partials, grid, d_msg_out);
+    finish_msg_kernel<<<1, kFinishThreads, 0, st>>>(d_partials, grid, d_msg_out);
     return 2;
 }
 
@@ -195,16 +208,35 @@ __global__ void eq_round_kernel(uint4 *eq, uint64_t half, const uint4 *point, in
     }
 }
 
-__global__ void eq_init_kernel(uint4 *eq) { eq[0] = make_uint4(1, 0, 0, 0); }
+// The first k rounds in one CTA (global writes of a round are visible to the
+// CTA's threads after the barrier).
+__global__ void __launch_bounds__(512) eq_small_kernel(uint4 *eq, const uint4 *point, int k) {
+    if (threadIdx.x == 0) eq[0] = make_uint4(1, 0, 0, 0);
+    __syncthreads();
+    for (int i = 0; i < k; ++i) {
+        const uint4 r = point[i];
+        const uint32_t half = 1u << i;
+        for (uint32_t j = threadIdx.x; j < half; j += blockDim.x) {
+            const uint4 p = eq[j];
+            const uint4 one = gf_mul(p, r);
+            eq[half + j] = one;
+            eq[j] = gf_add(p, one);
+        }
+        __syncthreads();
+    }
+}
+
+constexpr size_t kEqSmallRounds = 12;
 
 int launch_build_eq(const uint4 *d_point, size_t k, uint4 *d_out, cudaStream_t st) {
-    eq_init_kernel<<<1, 1, 0, st>>>(d_out);
-    for (size_t i = 0; i < k; ++i) {
+    const size_t k0 = std::min(k, kEqSmallRounds);
+    eq_small_kernel<<<1, 512, 0, st>>>(d_out, d_point, (int)k0);
+    for (size_t i = k0; i < k; ++i) {
         const uint64_t half = (uint64_t)1 << i;
         const unsigned grid = (unsigned)std::min<uint64_t>((half + 255) / 256, 8192);
         eq_round_kernel<<<std::max(grid, 1u), 256, 0, st>>>(d_out, half, d_point, (int)i);
     }
-    return (int)k + 1;
+    return (int)(k - k0) + 1;
 }
 
 // sv[j] = sum_y eq[y] * bit_j(P[y]) (src/ligerito.rs:317-375).  128 threads
@@ -242,11 +274,22 @@ __global__ void __launch_bounds__(128) sv_fold_kernel(const uint4 *packed, const
     partials[(uint64_t)blockIdx.x * 128 + j] = acc;
 }
 
-__global__ void sv_finish_kernel(const uint4 *partials, int n_ctas, uint4 *sv) {
-    const int j = threadIdx.x;
+// 1024 threads: thread (g, j) XORs output j of partials g, g + 8, ...; the 8
+// groups then combine in shared memory.
+constexpr int kSvFinishGroups = 8;
+__global__ void __launch_bounds__(128 * kSvFinishGroups) sv_finish_kernel(const uint4 *partials,
+                                                                          int n_ctas, uint4 *sv) {
+    __shared__ uint4 red[kSvFinishGroups][128];
+    const int j = threadIdx.x & 127, g = threadIdx.x >> 7;
     uint4 acc = make_uint4(0, 0, 0, 0);
-    for (int c = 0; c < n_ctas; ++c) acc = gf_add(acc, partials[(uint64_t)c * 128 + j]);
-    sv[j] = acc;
+    for (int c = g; c < n_ctas; c += kSvFinishGroups)
+        acc = gf_add(acc, partials[(uint64_t)c * 128 + j]);
+    red[g][j] = acc;
+    __syncthreads();
+    if (g == 0) {
+        for (int k = 1; k < kSvFinishGroups; ++k) acc = gf_add(acc, red[k][j]);
+        sv[j] = acc;
+    }
 }
 
 size_t sv_partials_bytes(size_t n, int num_sms) {
@@ -260,7 +303,7 @@ int launch_sv_fold(const uint4 *d_packed, const uint4 *d_eq, size_t n, uint64_t 
     const int grid = (int)std::max<uint64_t>(1, std::min<uint64_t>(tiles, (uint64_t)num_sms * 4));
     uint4 *parts = reinterpret_cast<uint4 *>(d_partials);
     sv_fold_kernel<<<grid, 128, 0, st>>>(d_packed, d_eq, n, parts);
-    sv_finish_kernel<<<1, 128, 0, st>>>(parts, grid, d_sv);
+    sv_finish_kernel<<<1, 128 * kSvFinishGroups, 0, st>>>(parts, grid, d_sv);
     return 2;
 }
 

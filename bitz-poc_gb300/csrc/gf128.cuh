@@ -100,6 +100,22 @@ BZ_HD uint4 gf_reduce(const gf_wide &r) {
 
 BZ_HD uint4 gf_mul(uint4 a, uint4 b) { return gf_reduce(gf_mul_wide(a, b)); }
 
+// t * X^e for 0 <= e < 128: t shifted left by e bits into 256 bits, reduced.
+BZ_HD uint4 gf_mul_xpow(uint4 t, uint32_t e) {
+    const uint64_t lo = lo64(t), hi = hi64(t);
+    const uint32_t s = e & 63;
+    const uint64_t a0 = lo << s;
+    const uint64_t a1 = s ? (hi << s) | (lo >> (64 - s)) : hi;
+    const uint64_t a2 = s ? hi >> (64 - s) : 0;
+    gf_wide w;
+    const bool up = e >= 64;
+    w.w[0] = up ? 0 : a0;
+    w.w[1] = up ? a0 : a1;
+    w.w[2] = up ? a1 : a2;
+    w.w[3] = up ? a2 : 0;
+    return gf_reduce(w);
+}
+
 // ---------------------------------------------------------------------------
 // Variable x constant with few set bits: XOR of v << s over the set bits s of
 // the constant t (t = {t0 bits 0..63, t1 bits 64..127}).  The loop trip count

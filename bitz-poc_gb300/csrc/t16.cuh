@@ -28,13 +28,7 @@ static __device__ __noinline__ void t16_build(uint4 *tbl, uint4 *bases, const ui
     const int tid = threadIdx.x, nthr = blockDim.x;
     for (int j = tid; j < 128 * n_tw; j += nthr) {
         const int i = j >> 7, e = j & 127;
-        uint4 xe = make_uint4(0, 0, 0, 0);
-        const uint32_t bit = 1u << (e & 31);
-        if (e < 32) xe.x = bit;
-        else if (e < 64) xe.y = bit;
-        else if (e < 96) xe.z = bit;
-        else xe.w = bit;
-        bases[j] = gf_mul(ts[i], xe);  // t * X^e
+        bases[j] = gf_mul_xpow(ts[i], (uint32_t)e);  // t * X^e
     }
     __syncthreads();
     for (int u = tid; u < 256 * n_tw; u += nthr) {
