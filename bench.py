@@ -551,12 +551,14 @@ def _bench_open(ctx, bz, msg, params):
         return statistics.median(ts[1:]) * 1e3, min(ts[1:]) * 1e3, out
 
     prove_ms, prove_min, proof = timed(lambda t: bz.prove(t, pd, msg, b, [1, 2], cfg, ctx))
+    prove_c_ms, _, _ = timed(lambda t: bz.prove(t, pd, msg, b, [1, 2], cfg, ctx, decode=False))
     blob = codec.encode_ligerito(proof)
     l0_cfg = bz.L0Config(initial_k=params.log_batch_size,
                          recursive_k0=params.log_batch_size // 2, log_inv_rate1=2,
                          grinding_bits0=16, queries0=148, hash_kind=HASH)
     l0_ms, l0_min, _ = timed(lambda t: bz.open_l0(t, pd, msg, b, [1, 2], l0_cfg, ctx))
-    info = {"prove_ms": prove_ms, "prove_ms_min": prove_min, "proof_bytes": len(blob),
+    info = {"prove_ms": prove_ms, "prove_ms_min": prove_min, "prove_c_abi_ms": prove_c_ms,
+            "proof_bytes": len(blob),
             "open_l0_ms": l0_ms, "open_l0_ms_min": l0_min, "config": OPEN_CONFIG_TEXT}
     # proof-of-work search alone: hashes scanned >= smallest nonce + 1
     pw = []

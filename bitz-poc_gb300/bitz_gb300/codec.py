@@ -131,14 +131,14 @@ def _view(p: LigeritoProof):
 
 
 def _rows_from(rv: RowsView) -> list:
-    out, off = [], 0
-    for i in range(rv.n_rows):
-        n = rv.row_lens[i]
-        a = np.ctypeslib.as_array(rv.data, shape=(2 * (off + n),))[2 * off:] if n else \
-            np.zeros(0, np.uint64)
-        out.append(a.reshape(-1, 2).copy())
-        off += n
-    return out
+    if not rv.n_rows:
+        return []
+    lens = np.ctypeslib.as_array(rv.row_lens, shape=(rv.n_rows,)).astype(np.int64)
+    total = int(lens.sum())
+    if not total:
+        return [np.zeros((0, 2), np.uint64) for _ in range(rv.n_rows)]
+    flat = np.ctypeslib.as_array(rv.data, shape=(2 * total,)).reshape(total, 2).copy()
+    return np.split(flat, np.cumsum(lens)[:-1])
 
 
 def _hashes_from(n, ptr) -> np.ndarray:

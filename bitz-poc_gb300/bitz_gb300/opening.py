@@ -177,10 +177,35 @@ class LigeritoConfig:
         return c, keep
 
 
+class ProofHandle:
+    """An undecoded bz_ligerito_proof (host memory); ``decode`` converts and frees it."""
+
+    def __init__(self, h):
+        self.h = h
+
+    def decode(self):
+        from .codec import _decoded
+
+        h, self.h = self.h, None
+        return _decoded(h)
+
+    def free(self):
+        if self.h:
+            lib().bz_ligerito_proof_free(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.free()
+        except Exception:
+            pass
+
+
 def prove(transcript: Blake3Transcript, data: ProverData, packed: DeviceArray,
-          basis: DeviceArray, target, cfg: LigeritoConfig, ctx: Context | None = None):
-    """The LigeritoProof of ``target`` against the commitment in ``data``."""
-    from .codec import _decoded
+          basis: DeviceArray, target, cfg: LigeritoConfig, ctx: Context | None = None,
+          decode: bool = True):
+    """The LigeritoProof of ``target`` against the commitment in ``data``
+    (with ``decode=False``, the undecoded ProofHandle)."""
 
     ctx = ctx or data.ctx or default_context()
     t = np.ascontiguousarray(np.asarray(target, dtype=np.uint64).reshape(2))
@@ -190,4 +215,5 @@ def prove(transcript: Blake3Transcript, data: ProverData, packed: DeviceArray,
                                               packed.ptr, basis.ptr, ptr(t), ctypes.byref(c),
                                               ctypes.byref(h)))
     del keep
-    return _decoded(h)
+    ph = ProofHandle(h)
+    return ph.decode() if decode else ph

@@ -77,7 +77,8 @@ struct Cursor {
         if (!u64(c)) return false;
         return item == 0 || c <= (n - cur) / item;
     }
-    bool words(std::vector<uint64_t> &out, uint64_t n_words) {
+    template <class Vec>
+    bool words(Vec &out, uint64_t n_words) {
         out.reserve(out.size() + n_words);
         for (uint64_t i = 0; i < n_words; ++i) {
             uint64_t w;

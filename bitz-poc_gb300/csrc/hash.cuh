@@ -17,14 +17,30 @@ __device__ __forceinline__ uint32_t rotr(uint32_t x, int n) { return __funnelshi
 // The two c += d additions are written as multiply-adds by a runtime 1
 // (`one`, read from constant memory so the compiler cannot fold it): they
 // then issue on the FMA pipe instead of the ALU pipe, which BLAKE3's xors and
-// rotates otherwise saturate.
+// rotates otherwise saturate.  BZ_B3_FMA_ADDS (0, 1 or 2) moves that many of
+// the two a += b + m additions to the FMA pipe as well (two multiply-adds
+// each instead of one three-input add); with both moved the leaf hashing of
+// a 2^24-element commit takes 0.57 ms instead of 0.67 ms on GB300.
+#ifndef BZ_B3_FMA_ADDS
+#define BZ_B3_FMA_ADDS 2
+#endif
+#if BZ_B3_FMA_ADDS >= 1
+#define BZ_B3ADD1(a, b, x) (s##a = (x) * one + (s##b * one + s##a))
+#else
+#define BZ_B3ADD1(a, b, x) (s##a = s##a + s##b + (x))
+#endif
+#if BZ_B3_FMA_ADDS >= 2
+#define BZ_B3ADD2(a, b, x) (s##a = (x) * one + (s##b * one + s##a))
+#else
+#define BZ_B3ADD2(a, b, x) (s##a = s##a + s##b + (x))
+#endif
 #define BZ_B3G(a, b, c, d, x, y)          \
     do {                                  \
-        s##a = s##a + s##b + (x);         \
+        BZ_B3ADD1(a, b, x);               \
         s##d = rotr(s##d ^ s##a, 16);     \
         s##c = s##d * one + s##c;         \
         s##b = rotr(s##b ^ s##c, 12);     \
-        s##a = s##a + s##b + (y);         \
+        BZ_B3ADD2(a, b, y);               \
         s##d = rotr(s##d ^ s##a, 8);      \
         s##c = s##d * one + s##c;         \
         s##b = rotr(s##b ^ s##c, 7);      \

@@ -36,6 +36,7 @@
 #include <algorithm>
 #include <new>
 #include <set>
+#include <utility>
 #include <vector>
 
 #include "../../include/bitz_gpu.h"
@@ -481,7 +482,7 @@ int bz_ligerito_prove(bz_ctx *ctx, bz_transcript *transcript, bz_commitment *c0,
     };
     if (!p) return finish(BZ_ERR_NOMEM);
     memcpy(p->initial_root, c0->root, 32);
-    p->initial = o->initial;
+    p->initial = std::move(o->initial);
     p->recursive_roots.insert(p->recursive_roots.end(), o->root1, o->root1 + 32);
     p->grinding_nonces.push_back(o->grinding_nonce);
     p->ood_values = o->ood_values;

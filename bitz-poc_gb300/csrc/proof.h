@@ -5,15 +5,40 @@
 #include <stddef.h>
 #include <stdint.h>
 
+#include <memory>
+#include <new>
+#include <utility>
 #include <vector>
 
 #include "../../include/bitz_gpu.h"
 
 namespace bzp {
 
+// Allocator whose resize leaves new elements uninitialised: opened rows are
+// written in full by a device copy right after the resize, so zero-filling
+// megabytes first would only touch the pages twice.
+template <class T>
+struct NoInitAlloc : std::allocator<T> {
+    template <class U>
+    struct rebind {
+        using other = NoInitAlloc<U>;
+    };
+    NoInitAlloc() = default;
+    template <class U>
+    NoInitAlloc(const NoInitAlloc<U> &) {}
+    template <class U>
+    void construct(U *p) {
+        ::new (static_cast<void *>(p)) U;
+    }
+    template <class U, class... Args>
+    void construct(U *p, Args &&...args) {
+        ::new (static_cast<void *>(p)) U(std::forward<Args>(args)...);
+    }
+};
+
 struct Rows {
     std::vector<size_t> lens;
-    std::vector<uint64_t> data;  // concatenated rows, 2 words per element
+    std::vector<uint64_t, NoInitAlloc<uint64_t>> data;  // concatenated rows, 2 words each
 };
 
 struct Level {
