@@ -629,28 +629,31 @@ def _bench_serve(ctx, bz, args):
     """Poisson commit-then-open requests with log2 sizes from a truncated
     geometric on [14, 26], admitted by free HBM (continuous batching); the
     arrival rate is swept to saturation.  Reports throughput and p50/p99
-    commit-to-opened latency per rate."""
+    commit-to-opened latency per rate.  The saturating point (1.5 x the
+    plain path's throughput) serves ``--serve-requests`` requests (10k by
+    default); the lighter loads a tenth of that, so the sweep stays within a
+    minute."""
     import numpy as np
     from bitz_gb300 import serve as S
 
     rng = np.random.default_rng(4)
-    n_req = args.serve_requests
-    sizes = _geometric_sizes(rng, n_req)
     # pinned host messages: one buffer of the largest size, prefixes reused
     import ctypes
 
     from bitz_gb300 import _lib
 
     L = _lib.lib()
-    max_n = 1 << int(sizes.max())
+    max_n = 1 << 26
     hp = ctypes.c_void_p()
     _lib.check(None, L.bz_host_alloc_pinned(16 * max_n, ctypes.byref(hp)))
     _lib.check(None, L.bz_chacha_fill_host(4, 0, hp, max_n, os.cpu_count() or 1))
-    total_elems = int(sum(1 << int(k) for k in sizes))
-    out = {"requests": n_req, "log2_size_mean": float(sizes.mean()), "unit": UNIT,
+    out = {"requests_at_saturation": args.serve_requests, "unit": UNIT,
            "sizes": "truncated geometric on [14,26], q=0.97", "rates": []}
-    # saturation throughput estimate from the plain path: elems/s ~ 3e9
     for load in (0.3, 0.6, 0.9, 1.5):
+        n_req = args.serve_requests if load >= 1.0 else max(args.serve_requests // 10, 50)
+        sizes = _geometric_sizes(rng, n_req)
+        total_elems = int(sum(1 << int(k) for k in sizes))
+        # saturation throughput estimate from the plain path: elems/s ~ 3e9
         lam = load * 3.0e9 / (total_elems / n_req)       # requests per second
         arrivals = np.cumsum(rng.exponential(1.0 / lam, n_req))
         with S.Server(ctx, n_slots=4) as srv:
@@ -688,7 +691,8 @@ def _bench_serve(ctx, bz, args):
             wall = time.perf_counter() - t0
         lat.sort()
         out["rates"].append({
-            "offered_load": load, "arrival_rate_per_s": lam, "throughput": total_elems / wall,
+            "offered_load": load, "requests": n_req, "log2_size_mean": float(sizes.mean()),
+            "arrival_rate_per_s": lam, "throughput": total_elems / wall,
             "p50_ms": lat[len(lat) // 2], "p99_ms": lat[min(len(lat) - 1, int(0.99 * len(lat)))],
             "wall_s": wall})
     L.bz_host_free_pinned(hp)
@@ -712,7 +716,8 @@ def main():
     ap.add_argument("--only-open", action="store_true",
                     help="the device commit loop and the opening leg only (profiling runs)")
     ap.add_argument("--log-n", type=int, default=None, help="override log2 elements")
-    ap.add_argument("--serve-requests", type=int, default=160)
+    ap.add_argument("--serve-requests", type=int, default=10000,
+                    help="requests per offered-load point of the serving sweep")
     args = ap.parse_args()
     if args.log_n is not None:
         global LOG_N, LOG_LANES, MSG_BYTES
