@@ -236,7 +236,11 @@ def run_gpu(args, ws, rank, local):
     import ctypes
 
     msg = bz.DeviceArray.chacha(SEED + rank, 1 << LOG_N, ctx)
-    schedule = ctx.autotune(params, reps=2) if not args.no_autotune else ctx.schedule(params)
+    if args.schedule is not None:
+        ctx.set_schedule(params, int(args.schedule, 0))
+        schedule = ctx.schedule(params)
+    else:
+        schedule = ctx.autotune(params, reps=2) if not args.no_autotune else ctx.schedule(params)
 
     def one_commit():
         h = ctypes.c_void_p()
@@ -711,6 +715,9 @@ def main():
     ap.add_argument("--skip-shapes", action="store_true")
     ap.add_argument("--skip-open", action="store_true")
     ap.add_argument("--no-autotune", action="store_true")
+    ap.add_argument("--schedule", default=None,
+                    help="fixed NTT schedule for the headline shape (e.g. 0x1002) instead of "
+                         "autotuning; profiling runs use the schedule a default run picked")
     ap.add_argument("--only-commit", action="store_true",
                     help="time the device commit loop only (profiling runs)")
     ap.add_argument("--only-open", action="store_true",

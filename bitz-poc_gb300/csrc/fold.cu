@@ -47,8 +47,9 @@ __device__ void cta_store_pair(gf_wide u0, gf_wide u2, uint64_t *out) {
 }
 
 // Dynamic shared memory of the kernels that multiply by one challenge r
-// through byte tables: the 64 KB table of r and its 128 basis products.
-constexpr size_t kRTableSmem = (size_t)kT16Entries * 16 + 128 * 16;
+// through byte tables: the 64 KB table of r and its 128 basis products
+// (padded to kT16Bases).
+constexpr size_t kRTableSmem = (size_t)kT16Entries * 16 + kT16Bases * 16;
 
 // Build the byte tables of r in shared memory (all threads; syncs inside).
 __device__ __forceinline__ const char *build_r_table(uint4 *smem, uint4 r) {

@@ -460,7 +460,7 @@ static bool table_pass_ok(int ell, int layer, int layers, int log_lanes, int log
 
 static size_t table_smem(int layers) {
     const int nt = layers == 2 ? 3 : 1;
-    return (size_t)nt * kT16Entries * 16 + (size_t)nt * 128 * 16;
+    return (size_t)nt * kT16Entries * 16 + (size_t)nt * kT16Bases * 16;
 }
 
 #define BZ_TAIL_ATTR(DT, DN, M)                                                           \

@@ -16,6 +16,10 @@
 namespace bz {
 
 constexpr int kT16Entries = 4096;  // 16 byte positions x 256 values
+// Scratch per twiddle for the 128 basis products t * X^e: groups of 8 (one
+// byte position) padded to 9 entries, so threads that read the same basis of
+// different byte positions hit different bank groups.
+constexpr int kT16Bases = 16 * 9;
 
 // Byte offset of entry (k, x) inside one table.
 __device__ __forceinline__ uint32_t t16_off(uint32_t k, uint32_t x) {
@@ -23,17 +27,21 @@ __device__ __forceinline__ uint32_t t16_off(uint32_t k, uint32_t x) {
 }
 
 // Build the tables of n_tw twiddles (ts[i]) into tbl[i * 4096 ..].  `bases`
-// is 128 * n_tw uint4 of scratch.  Called by all threads; syncs inside.
+// is kT16Bases * n_tw uint4 of scratch.  Called by all threads; syncs inside.
+// Thread u builds the 16 entries (k, hi * 16 + lo) of byte position
+// k = u mod 16: the 8 threads of a quarter-warp take 8 different byte
+// positions, so both their basis reads and their table writes fall in 8
+// different bank groups.
 static __device__ __noinline__ void t16_build(uint4 *tbl, uint4 *bases, const uint4 *ts, int n_tw) {
     const int tid = threadIdx.x, nthr = blockDim.x;
     for (int j = tid; j < 128 * n_tw; j += nthr) {
         const int i = j >> 7, e = j & 127;
-        bases[j] = gf_mul_xpow(ts[i], (uint32_t)e);  // t * X^e
+        bases[i * kT16Bases + (e >> 3) * 9 + (e & 7)] = gf_mul_xpow(ts[i], (uint32_t)e);
     }
     __syncthreads();
     for (int u = tid; u < 256 * n_tw; u += nthr) {
-        const int i = u >> 8, k = (u >> 4) & 15, hi = u & 15;
-        const uint4 *b = bases + i * 128 + 8 * k;
+        const int i = u >> 8, k = u & 15, hi = (u >> 4) & 15;
+        const uint4 *b = bases + i * kT16Bases + 9 * k;
         uint4 H = make_uint4(0, 0, 0, 0);
 #pragma unroll
         for (int q = 0; q < 4; ++q)
