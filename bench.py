@@ -515,9 +515,11 @@ def _bench_shapes(ctx, bz):
 
 def open_config(log_lanes: int) -> dict:
     """The opening leg's ProverConfig for a 2^log_lanes x 2^log_lanes witness."""
+    block1 = 1 << (log_lanes - log_lanes // 2 + 2)   # level-1 codeword length
     return dict(initial_k=log_lanes, recursive_ks=[log_lanes // 2],
-                log_inv_rates=[LOG_INV_RATE, 2], queries=[148, 148], grinding_bits=[16, 16],
-                fold_grinding_bits=None, ood_samples=None, hash_kind=HASH)
+                log_inv_rates=[LOG_INV_RATE, 2], queries=[148, min(148, block1 // 2)],
+                grinding_bits=[16, 16], fold_grinding_bits=None, ood_samples=None,
+                hash_kind=HASH)
 
 
 
