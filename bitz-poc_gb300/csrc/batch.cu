@@ -204,7 +204,15 @@ int bz_autotune(bz_ctx *ctx, const bz_params *params, int reps, uint32_t *chosen
     for (int d = 0; d <= std::min(4, b); ++d) {
         for (uint32_t r2 : {0u, (uint32_t)SCHED_RADIX2}) {
             if (d == 0) {
-                cands.push_back(r2);
+                // byte tables for every layer: plain, prefetching, 256-thread and
+                // register-capped CTAs, each also as a two-stream pipeline whose
+                // leaf hashing can share SMs with the capped table passes
+                for (uint32_t extra : {0u, (uint32_t)SCHED_PREFETCH,
+                                       (uint32_t)(SCHED_PREFETCH | SCHED_SMALL_CTA),
+                                       (uint32_t)SCHED_SMALL_CTA,
+                                       (uint32_t)(SCHED_PREFETCH | SCHED_SMALL_CTA | SCHED_LEAN)})
+                    for (uint32_t pipe = 0; pipe < 4; ++pipe)
+                        cands.push_back(r2 | extra | (pipe << SCHED_PIPE_SHIFT));
                 continue;
             }
             for (uint32_t mode = 0; mode < 3; ++mode) {

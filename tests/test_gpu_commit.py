@@ -48,7 +48,8 @@ SCHEDULES = [0, 1, 2, 3, 4, 0x10, 0x13, 0x20,
              0x52, 0x43 | (1 << 7), 0x44,
              0x200 | 2, (1 << 10) | 2, (2 << 10) | 0x200 | 2, (3 << 10) | 0x200 | 2,
              (2 << 10) | 0x200 | 3 | (1 << 7), (1 << 10) | 0x10 | 2, (3 << 10) | 0x200 | 0x11,
-             0x1000 | 2, 0x1200 | 2, 0x1000 | (1 << 10) | 2, 0x1000 | 0, 0x3602, 0x3a03]
+             0x1000 | 2, 0x1200 | 2, 0x1000 | (1 << 10) | 2, 0x1000 | 0, 0x3602, 0x3a03,
+             (1 << 10), (2 << 10) | 0x200, (3 << 10) | 0x3200, 0x1200 | (1 << 10), 0x3200]
 
 
 @pytest.mark.parametrize("schedule", SCHEDULES)
