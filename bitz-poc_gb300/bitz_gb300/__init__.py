@@ -25,3 +25,4 @@ from .transcript import Blake3Transcript, ZincChallenger, blake3_xof, pow_first_
 from .opening import L0Config, L0Opening, LigeritoConfig, open_l0, prove  # noqa: F401,E402
 from . import codec  # noqa: F401,E402
 from .binary_pcs import BinaryPcs, BitMleOpening, Round0Prover  # noqa: F401,E402
+from . import ingest  # noqa: F401,E402

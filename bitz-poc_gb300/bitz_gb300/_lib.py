@@ -129,6 +129,10 @@ _SIGS = {
     "bz_read_round0": (_I, [_P, _P, ctypes.POINTER(_I), ctypes.POINTER(_U64)]),
     "bz_read_ring_switch": (_I, [_P, _P]),
     "bz_read_ligerito": (_I, [_P, _PP]),
+    "bz_repack_leaf_bits": (_I, [_P, _P, _U32, _U32, _P]),
+    "bz_pack_columns_from_rows": (_I, [_P, _P, _U32, _U32, _P]),
+    "bz_rows_from_packed_cols": (_I, [_P, _P, _U32, _U32, _P]),
+    "bz_commit_rows": (_I, [_P, _P, _U32, _U32, _U32, _U32, _U32, _PP, _P]),
     "bz_autotune": (_I, [_P, ctypes.POINTER(Params), _I, ctypes.POINTER(_U32)]),
     "bz_schedule_get": (_I, [_P, ctypes.POINTER(Params), ctypes.POINTER(_U32)]),
     "bz_schedule_set": (_I, [_P, ctypes.POINTER(Params), _U32]),

@@ -147,6 +147,14 @@ int launch_split_dot(const uint4 *d_p, const uint4 *d_tail, int lo, const uint4 
 int launch_eq_axpy(uint4 *d_b, const uint4 *d_tail, int lo, const uint4 *d_head, uint4 eta,
                    size_t n, cudaStream_t st);
 
+// Bit-matrix ingest (ingest.cu).
+int launch_repack_leaf_bits(const uint4 *d_cells, int row_vars, int col_vars, uint64_t *d_rows,
+                            unsigned int *d_bad, cudaStream_t st);
+int launch_pack_columns(const uint64_t *d_rows, int row_vars, int col_vars, uint64_t *d_packed,
+                        cudaStream_t st);
+int launch_unpack_columns(const uint64_t *d_packed, int row_vars, int col_vars, uint64_t *d_rows,
+                          cudaStream_t st);
+
 // One-time kernel attributes (large dynamic shared memory), called when a
 // context is created so no attribute call happens during graph capture.
 void init_ntt_kernels();

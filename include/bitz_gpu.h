@@ -512,6 +512,30 @@ int bz_pcs_open_bit_mle(bz_ctx *ctx, bz_transcript *transcript, bz_commitment *c
                         size_t point_len, const bz_ligerito_config *cfg, uint64_t s_v[256],
                         bz_ligerito_proof **out);
 
+/* ---- bit-matrix ingest ------------------------------------------------------ */
+/* A 2^row_vars x 2^col_vars bit matrix (IntegerMatrixLayout, src/pcs.rs:14-41;
+ * cell (b, c) at flat index (b << col_vars) | c).  "rows": per column c its
+ * bits packed 64 per word, W = ceil(2^row_vars / 64) words per column;
+ * "packed columns": ceil(2^col_vars / 64) groups of 2^row_vars words, bit k
+ * of word i of group g = column 64g + k's bit i.  All buffers on the device. */
+/* repack_leaf_bits (src/ligerito.rs:19-33): d_cells holds one u128 (2 words)
+ * per cell, each 0 or 1 (BZ_ERR_ARG otherwise, as the reference asserts). */
+int bz_repack_leaf_bits(bz_ctx *ctx, const uint64_t *d_cells, uint32_t row_vars,
+                        uint32_t col_vars, uint64_t *d_rows);
+/* pack_columns_from_rows / rows_from_packed_cols (src/ligerito.rs:655-717):
+ * 64 x 64 bit transposes. */
+int bz_pack_columns_from_rows(bz_ctx *ctx, const uint64_t *d_rows, uint32_t row_vars,
+                              uint32_t col_vars, uint64_t *d_packed_cols);
+int bz_rows_from_packed_cols(bz_ctx *ctx, const uint64_t *d_packed_cols, uint32_t row_vars,
+                             uint32_t col_vars, uint64_t *d_rows);
+/* commit_rs_flock_from_rows (src/ligerito_flock.rs:198-245): the packed
+ * message is the rows buffer read as {lo, hi} pairs (2^(row_vars - 7 +
+ * col_vars) elements); requires row_vars >= 7 and log_batch < that count's
+ * log. */
+int bz_commit_rows(bz_ctx *ctx, const uint64_t *d_rows, uint32_t row_vars, uint32_t col_vars,
+                   uint32_t log_inv_rate, uint32_t log_batch, uint32_t hash_kind,
+                   bz_commitment **out, uint8_t root[32]);
+
 /* ---- synthetic inputs --------------------------------------------------- */
 /* RFC 8439 ChaCha20 keystream words (key = seed LE u64 zero padded, nonce 0,
  * counter from 0), word i = keystream bytes [16 i, 16 i + 16). */
