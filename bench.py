@@ -47,6 +47,32 @@ WORKLOAD = {
 }
 MSG_BYTES = 16 << LOG_N
 ALG_BYTES_PER_WORD = 16 + (16 << LOG_INV_RATE)   # read message + write codeword
+SCHED_PIPE_BITS = 3 << 10                         # pipeline chunk count of a schedule
+# One GF(2^128) multiply by a block twiddle = 16 byte-table lookups of 16 B.
+T16_BYTES_PER_MUL = 16 * 16
+SMEM_BYTES_PER_CLK_PER_SM = 128
+# DRAM bytes (read + write) per codeword byte of one launch, from ncu
+# captures of the same kernels on GB300 (dram__bytes_read.sum +
+# dram__bytes_write.sum), with the profile they come from.
+NCU_TRAFFIC_PER_CW_BYTE = {}
+
+
+def table_pass_lookup_bytes(kernel: str, layer: int, log_positions_lanes: int) -> int:
+    """Shared-memory bytes read by the twiddle multiplies of one table pass
+    over 2^log_positions_lanes codeword elements starting at `layer`.
+
+    A radix-4 pass multiplies each quad 4 times (t_o twice, then t_a and
+    t_b), a radix-2 pass each pair once.  Block 0 of every layer has a zero
+    twiddle (the span of no evaluation is 0), so its quads skip the t_o and
+    t_a products and its pairs skip theirs."""
+    n = 1 << log_positions_lanes
+    if kernel.startswith("ntt_table_pass2"):
+        quads = n // 4
+        muls = 4 * quads - 3 * (quads >> layer)
+    else:
+        pairs = n // 2
+        muls = pairs - (pairs >> layer)
+    return muls * T16_BYTES_PER_MUL
 
 
 def _dist():
@@ -351,13 +377,24 @@ def run_gpu(args, ws, rank, local):
     out = None
     if rank == 0:
         # ---- per-kernel phase times and the roofline of the dominant kernel
+        # (a pipelined schedule overlaps its kernels on two streams, so its
+        # phase split is taken with the same kernels launched in sequence)
+        prof_schedule = schedule & ~SCHED_PIPE_BITS
+        if prof_schedule != schedule:
+            ctx.set_schedule(params, prof_schedule)
         phases, proot = ctx.commit_profile(msg, params)
+        if prof_schedule != schedule:
+            ctx.set_schedule(params, schedule)
         assert proot == root0
-        agg = {}
+        agg, lookup_bytes = {}, {}
         for name, ms in phases:
-            a = agg.setdefault(name, [0, 0.0])
+            kern, _, layer = name.partition("@")
+            a = agg.setdefault(kern, [0, 0.0])
             a[0] += 1
             a[1] += ms
+            if layer:
+                lookup_bytes.setdefault(kern, []).append(
+                    table_pass_lookup_bytes(kern, int(layer), LOG_N + LOG_INV_RATE))
         total_phase = sum(v[1] for v in agg.values())
         dom = max(agg.items(), key=lambda kv: kv[1][1])
         dom_name, (dom_n, dom_ms) = dom
@@ -371,6 +408,23 @@ def run_gpu(args, ws, rank, local):
             alg_bytes = cw_bytes
         peak, peak_kind = _peaks()
         achieved = alg_bytes / (dom_ms / dom_n / 1e3) / 1e9
+        traffic = None
+        if dom_name in NCU_TRAFFIC_PER_CW_BYTE:
+            traffic = NCU_TRAFFIC_PER_CW_BYTE[dom_name][0] * cw_bytes
+        smem = None
+        if dom_name in lookup_bytes:
+            import torch
+
+            sms = torch.cuda.get_device_properties(local).multi_processor_count
+            mhz = clk.get("sm_mhz") or clk.get("sm_max_mhz")
+            lb = sum(lookup_bytes[dom_name]) / len(lookup_bytes[dom_name])
+            s_ach = lb / (dom_ms / dom_n / 1e3) / 1e9
+            s_peak = SMEM_BYTES_PER_CLK_PER_SM * sms * mhz * 1e6 / 1e9 if mhz else None
+            smem = {"bound": "shared-memory pipe", "lookup_bytes_per_launch": lb,
+                    "achieved": s_ach, "peak": s_peak, "unit": "GB/s",
+                    "frac": s_ach / s_peak if s_peak else None,
+                    "peak_source": f"nominal {SMEM_BYTES_PER_CLK_PER_SM} B/clk/SM x {sms} SMs x "
+                                   f"median sampled SM clock {mhz} MHz"}
         commit_ms = statistics.median(step_ms)
         commit_gbs = ALG_BYTES_PER_WORD * (1 << LOG_N) / (commit_ms / 1e3) / 1e9
 
@@ -414,10 +468,13 @@ def run_gpu(args, ws, rank, local):
                     "pipelined": "upload of step i+1 overlaps the kernels of step i",
                     "sync_call_value": ws * args.steps * (1 << LOG_N) / (e2e_sync_ms / 1e3)},
             "roofline": {"bound": "hbm", "kernel": dom_name, "achieved": achieved, "peak": peak,
-                         "unit": "GB/s", "frac": achieved / peak, "traffic": None,
+                         "unit": "GB/s", "frac": achieved / peak, "traffic": traffic,
+                         "traffic_source": (NCU_TRAFFIC_PER_CW_BYTE[dom_name][1]
+                                            if traffic is not None else None),
                          "alg_bytes_per_launch": alg_bytes, "launch_ms": dom_ms / dom_n,
-                         "peak_source": peak_kind,
-                         "commit_alg_gbs": commit_gbs, "commit_frac": commit_gbs / peak},
+                         "peak_source": peak_kind, "phase_schedule": prof_schedule,
+                         "commit_alg_gbs": commit_gbs, "commit_frac": commit_gbs / peak,
+                         "smem": smem},
             "phases_ms": {k: round(v[1], 4) for k, v in agg.items()},
             "phase_share": {k: round(v[1] / total_phase, 4) for k, v in agg.items()},
             "clocks": clk, "gpu_launches": launches, "wall_s": wall,
@@ -494,6 +551,9 @@ def _bench_shapes(ctx, bz):
         p = bz.PcsParams(log_n + 7, LOG_INV_RATE, log_n // 2, HASH)
         m = bz.DeviceArray.chacha(log_n, 1 << log_n, ctx)
         sched = ctx.autotune(p, reps=1)
+        # phases of a pipelined schedule are split with its kernels in sequence
+        if sched & SCHED_PIPE_BITS:
+            ctx.set_schedule(p, sched & ~SCHED_PIPE_BITS)
         best = None
         for _ in range(reps):
             phases, root = ctx.commit_profile(m, p)
@@ -506,7 +566,8 @@ def _bench_shapes(ctx, bz):
         cw_bytes = 16 << (log_n + LOG_INV_RATE)
         out[f"2^{log_n}"] = {
             "value": (1 << log_n) / (tot / 1e3), "unit": UNIT, "ms": tot, "ntt_ms": ntt,
-            "merkle_ms": mk, "schedule": sched, "root": root.hex(),
+            "merkle_ms": mk, "schedule": sched, "phase_schedule": sched & ~SCHED_PIPE_BITS,
+            "root": root.hex(),
             "commit_alg_gbs": ALG_BYTES_PER_WORD * (1 << log_n) / (tot / 1e3) / 1e9,
             "merkle_read_gbs": cw_bytes / (mk / 1e3) / 1e9, "hbm_peak_gbs": peak}
         m.free()

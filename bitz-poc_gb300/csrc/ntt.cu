@@ -31,6 +31,7 @@
 
 #include <algorithm>
 #include <cstring>
+#include <string>
 
 #include "bz_internal.h"
 #include "gf128.cuh"
@@ -622,8 +623,13 @@ int launch_ntt(const Shape &s, uint32_t schedule, const uint4 *d_msg, uint4 *d_c
         launches += launch_table_pass(s, layer, layers, src, src_bits, d_cw, d_tw, 0, P, threads,
                                       st, num_sms, (schedule & SCHED_PREFETCH) != 0,
                                       (schedule & SCHED_LEAN) != 0);
-        mark(layers == 2 ? (src == d_msg ? "ntt_table_pass2_first" : "ntt_table_pass2")
-                         : (src == d_msg ? "ntt_table_pass1_first" : "ntt_table_pass1"));
+        if (log) {
+            // "<kernel>@<first layer>": the profile's reader counts the
+            // multiplies of each launch from its layer
+            std::string n = layers == 2 ? (src == d_msg ? "ntt_table_pass2_first" : "ntt_table_pass2")
+                                        : (src == d_msg ? "ntt_table_pass1_first" : "ntt_table_pass1");
+            log->mark((n + "@" + std::to_string(layer)).c_str());
+        }
         src = d_cw;
         src_bits = 62;
         layer += layers;

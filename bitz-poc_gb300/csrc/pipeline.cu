@@ -11,6 +11,7 @@
 #include <cuda_runtime.h>
 
 #include <algorithm>
+#include <string>
 
 #include "bz_internal.h"
 
@@ -46,7 +47,10 @@ int launch_commit_pipelined(const Shape &s, uint32_t schedule, const uint4 *d_ms
     const bool pf = (schedule & SCHED_PREFETCH) != 0, lean = (schedule & SCHED_LEAN) != 0;
     int launches =
         launch_table_pass(s, r, first, d_msg, b, d_cw, d_tw, 0, P, threads, st, num_sms, pf, lean);
-    if (log) log->mark(first == 2 ? "ntt_table_pass2_first" : "ntt_table_pass1_first");
+    if (log)
+        log->mark((std::string(first == 2 ? "ntt_table_pass2_first" : "ntt_table_pass1_first") +
+                   "@" + std::to_string(r))
+                      .c_str());
     for (int k = 0; k < chunks; ++k) {
         const uint64_t p0 = P / chunks * k, p1 = P / chunks * (k + 1);
         for (int layer = r + first; layer < table_end;) {
