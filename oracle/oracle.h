@@ -10,11 +10,14 @@
  * Parity status: the field is pinned to NIST GCM/GHASH known answers, SHA-256
  * to Python's hashlib, ChaCha20 to the `cryptography` package, BLAKE3 to the
  * BLAKE3 specification's published digests (single- and multi-chunk inputs);
- * the NTT / commit / Merkle / fold code follows the reference source line by
- * line (file:line cited beside each function) but has no reference-produced
- * golden file to compare with (the reference is Rust and no Rust toolchain
- * exists on either machine): for those functions parity is "unpinned" beyond
- * the reference's own self-consistency identities, which the tests restate.
+ * the NTT and the commit codeword to the Reed-Solomon encoding in the
+ * Lin-Chung-Han novel basis evaluated from its definition (a second,
+ * independent derivation in lch_definition.py).  The Merkle / fold code
+ * follows the reference source (file:line cited beside each function) but
+ * has no reference-produced golden file to compare with (the reference is
+ * Rust and no Rust toolchain exists on either machine): for those functions
+ * parity is "unpinned" beyond the reference's own self-consistency
+ * identities, which the tests restate.
  *
  * Element layout everywhere: a GF(2^128) element is two little-endian uint64
  * words {lo, hi}; arrays of n elements are uint64_t[2n].

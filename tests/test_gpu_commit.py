@@ -43,6 +43,23 @@ def test_commit_matches_oracle(oracle, ctx, lm, r, lb, kind):
         pd.free()
 
 
+@pytest.mark.parametrize("lm,r,lb", [(1, 1, 0), (4, 1, 0), (6, 2, 1), (8, 1, 2), (7, 3, 4)])
+def test_commit_codeword_equals_rs_definition(ctx, lm, r, lb):
+    """The device codeword against the Lin-Chung-Han novel-basis evaluation
+    computed from its definition (oracle/lch_definition.py), lane by lane."""
+    from oracle import lch_definition as D
+
+    rng = np.random.default_rng(0xDEF + lm)
+    msg = rng.integers(0, 2**64, (1 << lm, 2), dtype=np.uint64)
+    c, pd = _gpu_commit(msg, r, lb, 1, ctx)
+    try:
+        ints = [int(w[0]) | (int(w[1]) << 64) for w in msg]
+        got = [int(w[0]) | (int(w[1]) << 64) for w in pd.codeword.reshape(-1, 2)]
+        assert got == D.interleaved_codeword(ints, lb, r)
+    finally:
+        pd.free()
+
+
 SCHEDULES = [0, 1, 2, 3, 4, 0x10, 0x13, 0x20,
              2 | (1 << 7), 3 | (2 << 7), 0x42, 0x41, 0x43, 0x42 | (1 << 7), 0x42 | (2 << 7),
              0x52, 0x43 | (1 << 7), 0x44,
