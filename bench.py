@@ -54,7 +54,11 @@ SMEM_BYTES_PER_CLK_PER_SM = 128
 # DRAM bytes (read + write) per codeword byte of one launch, from ncu
 # captures of the same kernels on GB300 (dram__bytes_read.sum +
 # dram__bytes_write.sum), with the profile they come from.
-NCU_TRAFFIC_PER_CW_BYTE = {}
+NCU_TRAFFIC_PER_CW_BYTE = {
+    "ntt_table_pass2": (1.940, "profiles/traffic_commit_2e24.md (mean of the 5 in-place passes)"),
+    "ntt_table_pass2_first": (1.427, "profiles/traffic_commit_2e24.md"),
+    "b3_leaves_chunked": (1.073, "profiles/traffic_commit_2e24.md"),
+}
 
 
 def table_pass_lookup_bytes(kernel: str, layer: int, log_positions_lanes: int) -> int:
