@@ -103,6 +103,35 @@ struct TablePassArgs {
     uint64_t task_base; // first task (restricts the pass to a range of positions)
 };
 
+// Twiddles of the blocks a CTA visits, staged in shared memory kTwWindow
+// blocks at a time by all threads, so a table rebuild at a block boundary
+// reads them from shared memory instead of waiting on one thread's global
+// loads.  win[0], win[1] = first staged block and count (set by thread 0 after
+// a barrier); NT = 3 stages (t_o, t_a, t_b) per block, NT = 1 stages t.
+constexpr int kTwWindow = 64;
+template <int NT>
+__device__ __forceinline__ const uint4 *tw_window(const uint4 *tw, int layer, uint64_t B,
+                                                  uint64_t b_last, uint4 *buf, uint64_t *win) {
+    uint64_t b0 = win[0];
+    const uint64_t n0 = win[1];
+    if (B >= b0 + n0) {  // uniform: every thread read the same win[] after a barrier
+        const uint64_t n = min((uint64_t)kTwWindow, b_last + 1 - B);
+        for (uint64_t j = threadIdx.x; j < n * NT; j += blockDim.x) {
+            const uint64_t b = B + j / NT;
+            const int w = (int)(j % NT);
+            buf[j] = w == 0 ? tw[((uint64_t)1 << layer) + b]
+                            : tw[((uint64_t)1 << (layer + 1)) + 2 * b + (uint64_t)(w - 1)];
+        }
+        __syncthreads();
+        if (threadIdx.x == 0) {
+            win[0] = B;
+            win[1] = n;
+        }
+        b0 = B;
+    }
+    return buf + (B - b0) * NT;
+}
+
 // LAYERS = 2: radix-4 quad (a, b, c, d) at positions B*4Q + g*Q + rr:
 //   layer l   : (a,c), (b,d) with t_o = twiddle(l, B)
 //   layer l+1 : (a,b) with t_a = twiddle(l+1, 2B), (c,d) with t_b = twiddle(l+1, 2B+1)
@@ -115,8 +144,10 @@ __global__ void __launch_bounds__(THREADS, 1) ntt_table_pass(TablePassArgs a) {
     constexpr int NT = LAYERS == 2 ? 3 : 1;
     uint4 *tbl = smem;
     uint4 *bases = smem + NT * kT16Entries;
-    __shared__ uint4 ts[3];
+    __shared__ uint4 tw_buf[kTwWindow * NT];
+    __shared__ uint64_t win[2];
     __shared__ int tz[3];
+    if (threadIdx.x == 0) win[0] = win[1] = 0;
 
     T16Lane lane_ctx;
     lane_ctx.init();
@@ -131,6 +162,7 @@ __global__ void __launch_bounds__(THREADS, 1) ntt_table_pass(TablePassArgs a) {
     const uint64_t chunks = a.n_tasks / blockDim.x;
     const uint64_t c_beg = chunks * blockIdx.x / gridDim.x;
     const uint64_t c_end = chunks * (blockIdx.x + 1) / gridDim.x;
+    const uint64_t b_last = (a.task_base + c_end * blockDim.x - 1) >> log_task_per_b;
     int64_t cur_b = -1;
 
     for (uint64_t c = c_beg; c < c_end; ++c) {
@@ -138,18 +170,9 @@ __global__ void __launch_bounds__(THREADS, 1) ntt_table_pass(TablePassArgs a) {
         const uint64_t B = task >> log_task_per_b;  // uniform across the CTA
         if ((int64_t)B != cur_b) {
             __syncthreads();
-            if (threadIdx.x == 0) {
-                if (LAYERS == 2) {
-                    ts[0] = a.tw[((uint64_t)1 << a.layer) + B];
-                    ts[1] = a.tw[((uint64_t)1 << (a.layer + 1)) + 2 * B];
-                    ts[2] = a.tw[((uint64_t)1 << (a.layer + 1)) + 2 * B + 1];
-                } else {
-                    ts[0] = a.tw[((uint64_t)1 << a.layer) + B];
-                }
-                for (int i = 0; i < NT; ++i) tz[i] = gf_is_zero(ts[i]);
-            }
-            __syncthreads();
-            t16_build(tbl, bases, ts, NT);
+            const uint4 *ts = tw_window<NT>(a.tw, a.layer, B, b_last, tw_buf, win);
+            if (threadIdx.x < NT) tz[threadIdx.x] = gf_is_zero(ts[threadIdx.x]);
+            t16_build(tbl, bases, ts, NT);  // its barriers publish tz
             cur_b = (int64_t)B;
         }
         const uint64_t rr = (task >> a.log_lanes) & q_mask;
@@ -197,8 +220,10 @@ __global__ void __launch_bounds__(THREADS, MINB) ntt_table_pass2_pf(TablePassArg
     extern __shared__ uint4 smem[];
     uint4 *tbl = smem;
     uint4 *bases = smem + 3 * kT16Entries;
-    __shared__ uint4 ts[3];
+    __shared__ uint4 tw_buf[kTwWindow * 3];
+    __shared__ uint64_t win[2];
     __shared__ int tz[3];
+    if (threadIdx.x == 0) win[0] = win[1] = 0;
     T16Lane8 lane_ctx;
     lane_ctx.init();
     const int log_q = a.ell - a.layer - 2;
@@ -209,6 +234,7 @@ __global__ void __launch_bounds__(THREADS, MINB) ntt_table_pass2_pf(TablePassArg
     const uint64_t chunks = a.n_tasks / blockDim.x;
     const uint64_t c_beg = chunks * blockIdx.x / gridDim.x;
     const uint64_t c_end = chunks * (blockIdx.x + 1) / gridDim.x;
+    const uint64_t b_last = (a.task_base + c_end * blockDim.x - 1) >> log_task_per_b;
     int64_t cur_b = -1;
     auto src_index = [&](uint64_t task, int g) -> uint64_t {
         const uint64_t B = task >> log_task_per_b;
@@ -235,14 +261,9 @@ __global__ void __launch_bounds__(THREADS, MINB) ntt_table_pass2_pf(TablePassArg
         }
         if ((int64_t)B != cur_b) {
             __syncthreads();
-            if (threadIdx.x == 0) {
-                ts[0] = a.tw[((uint64_t)1 << a.layer) + B];
-                ts[1] = a.tw[((uint64_t)1 << (a.layer + 1)) + 2 * B];
-                ts[2] = a.tw[((uint64_t)1 << (a.layer + 1)) + 2 * B + 1];
-                for (int i = 0; i < 3; ++i) tz[i] = gf_is_zero(ts[i]);
-            }
-            __syncthreads();
-            t16_build(tbl, bases, ts, 3);
+            const uint4 *ts = tw_window<3>(a.tw, a.layer, B, b_last, tw_buf, win);
+            if (threadIdx.x < 3) tz[threadIdx.x] = gf_is_zero(ts[threadIdx.x]);
+            t16_build(tbl, bases, ts, 3);  // its barriers publish tz
             cur_b = (int64_t)B;
         }
         const char *T0 = reinterpret_cast<const char *>(tbl);
