@@ -61,7 +61,7 @@ NCU_TRAFFIC_PER_CW_BYTE = {
 }
 
 
-def table_pass_lookup_bytes(kernel: str, layer: int, log_positions_lanes: int) -> int:
+def table_pass_lookup_bytes(kernel: str, layer: int, log_positions_lanes: int) -> int | None:
     """Shared-memory bytes read by the twiddle multiplies of one table pass
     over 2^log_positions_lanes codeword elements starting at `layer`.
 
@@ -70,6 +70,8 @@ def table_pass_lookup_bytes(kernel: str, layer: int, log_positions_lanes: int) -
     twiddle (the span of no evaluation is 0), so its quads skip the t_o and
     t_a products and its pairs skip theirs."""
     n = 1 << log_positions_lanes
+    if kernel.endswith("_nw"):
+        return None   # compact 4-byte tables for narrow twiddles: not this model
     if kernel.startswith("ntt_table_pass2"):
         quads = n // 4
         muls = 4 * quads - 3 * (quads >> layer)
@@ -416,7 +418,7 @@ def run_gpu(args, ws, rank, local):
         if dom_name in NCU_TRAFFIC_PER_CW_BYTE:
             traffic = NCU_TRAFFIC_PER_CW_BYTE[dom_name][0] * cw_bytes
         smem = None
-        if dom_name in lookup_bytes:
+        if dom_name in lookup_bytes and None not in lookup_bytes[dom_name]:
             import torch
 
             sms = torch.cuda.get_device_properties(local).multi_processor_count

@@ -208,6 +208,7 @@ int bz_autotune(bz_ctx *ctx, const bz_params *params, int reps, uint32_t *chosen
                 // register-capped CTAs, each also as a two-stream pipeline whose
                 // leaf hashing can share SMs with the capped table passes
                 for (uint32_t extra : {0u, (uint32_t)SCHED_PREFETCH,
+                                       (uint32_t)(SCHED_PREFETCH | SCHED_NARROW),
                                        (uint32_t)(SCHED_PREFETCH | SCHED_SMALL_CTA),
                                        (uint32_t)SCHED_SMALL_CTA,
                                        (uint32_t)(SCHED_PREFETCH | SCHED_SMALL_CTA | SCHED_LEAN)})
@@ -222,6 +223,7 @@ int bz_autotune(bz_ctx *ctx, const bz_params *params, int reps, uint32_t *chosen
                                     (mode << SCHED_MODE_SHIFT));
             }
             cands.push_back((uint32_t)d | r2 | SCHED_PREFETCH);
+            cands.push_back((uint32_t)d | r2 | SCHED_PREFETCH | SCHED_NARROW);
             cands.push_back((uint32_t)d | r2 | SCHED_PREFETCH | SCHED_SMALL_CTA);
             for (uint32_t small : {0u, (uint32_t)SCHED_SMALL_CTA})
                 for (uint32_t pipe = 0; pipe < 4; ++pipe)

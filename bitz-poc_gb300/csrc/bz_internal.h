@@ -47,7 +47,8 @@ struct LaunchLog {
 // bit 4 = use radix-2 passes only for the table layers, bit 5 = force the
 // generic one-layer-per-launch kernels (reference / fallback path), bit 6 =
 // fuse the last table layers with the deep layers into one tail pass, bits
-// 7..8 = narrow-multiply variant (0 shifts, 1 wide multiplies, 2 alternate).
+// 7..8 = narrow-multiply variant (0 shifts, 1 wide multiplies, 2 alternate),
+// bit 14 = radix-4 passes with narrow (<= 25-bit) twiddles use compact tables.
 enum : uint32_t {
     SCHED_DEEP_MASK = 0xF,
     SCHED_RADIX2 = 0x10,
@@ -58,6 +59,7 @@ enum : uint32_t {
     SCHED_PIPE_SHIFT = 10,        // bits 10..11: log2 of the pipeline chunk count
     SCHED_PREFETCH = 0x1000,      // radix-4 table passes double-buffer their loads
     SCHED_LEAN = 0x2000,          // cap table-pass registers (room for co-resident CTAs)
+    SCHED_NARROW = 0x4000,        // compact 32-bit tables for the deepest layers' twiddles
 };
 uint32_t default_schedule(const Shape &s);
 
@@ -74,7 +76,9 @@ int launch_ntt(const Shape &s, uint32_t schedule, const uint4 *d_msg, uint4 *d_c
 // blocks), used by the pipelined commit.
 int launch_table_pass(const Shape &s, int layer, int layers, const uint4 *src, int src_bits,
                       uint4 *dst, const uint4 *tw, uint64_t p0, uint64_t p1, int threads,
-                      cudaStream_t st, int num_sms, bool prefetch = false, bool lean = false);
+                      cudaStream_t st, int num_sms, uint32_t schedule);
+// Bit length of the widest twiddle of `layer` in the ell-layer transform.
+int twiddle_bits(int ell, int layer);
 int launch_deep_range(const Shape &s, int deep, int mode, const uint4 *src, int src_bits,
                       uint4 *dst, const uint4 *tw, uint64_t p0, uint64_t p1, cudaStream_t st,
                       int num_sms);

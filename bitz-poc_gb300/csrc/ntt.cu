@@ -31,6 +31,8 @@
 
 #include <algorithm>
 #include <cstring>
+#include <map>
+#include <mutex>
 #include <string>
 
 #include "bz_internal.h"
@@ -42,9 +44,10 @@ namespace bz {
 // ===========================================================================
 // Host: normalized subspace-polynomial rows and the twiddle heap.
 // ===========================================================================
-std::vector<uint64_t> twiddle_heap(int ell) {
-    // evals[i][k], i < ell, k < ell - i (additive_ntt_f128.rs:66-100) for the
-    // basis {1, x, .., x^(ell-1)} (:136-140).
+// evals[i][k], i < ell, k < ell - i (additive_ntt_f128.rs:66-100) for the
+// basis {1, x, .., x^(ell-1)} (:136-140), element (i, k) at words
+// 2 * (i * ell + k) and + 1.
+static std::vector<uint64_t> normalized_evals(int ell) {
     std::vector<uint64_t> ev(2 * (size_t)ell * ell, 0);
     auto at = [&](int i, int k) { return &ev[2 * ((size_t)i * ell + k)]; };
     for (int k = 0; k < ell; ++k) {
@@ -68,6 +71,12 @@ std::vector<uint64_t> twiddle_heap(int ell) {
             at(i, k)[1] = t[1];
         }
     }
+    return ev;
+}
+
+std::vector<uint64_t> twiddle_heap(int ell) {
+    std::vector<uint64_t> ev = normalized_evals(ell);
+    auto at = [&](int i, int k) { return &ev[2 * ((size_t)i * ell + k)]; };
     std::vector<uint64_t> heap(2 * ((size_t)1 << ell) + 2, 0);
     for (int l = 0; l < ell; ++l) {
         const size_t base = (size_t)1 << l;
@@ -83,6 +92,32 @@ std::vector<uint64_t> twiddle_heap(int ell) {
         }
     }
     return heap;
+}
+
+// Bit length of the widest twiddle of `layer`: twiddle(layer, b) is the XOR
+// of evals[ell - layer - 1][1 + j] over the set bits j < layer of b, so it
+// is no wider than its widest generator.  Deep layers have narrow twiddles
+// (about ell, 2 ell - 3, 4 ell - 11 bits at depths 0, 1, 2).
+int twiddle_bits(int ell, int layer) {
+    static std::mutex mu;
+    static std::map<int, std::vector<int>> cache;
+    std::lock_guard<std::mutex> g(mu);
+    auto it = cache.find(ell);
+    if (it == cache.end()) {
+        const std::vector<uint64_t> ev = normalized_evals(ell);
+        std::vector<int> bits(ell, 0);
+        for (int l = 0; l < ell; ++l) {
+            const int row = ell - l - 1;
+            for (int k = 1; k <= l; ++k) {
+                const uint64_t lo = ev[2 * ((size_t)row * ell + k)];
+                const uint64_t hi = ev[2 * ((size_t)row * ell + k) + 1];
+                const int b = hi ? 128 - __builtin_clzll(hi) : (lo ? 64 - __builtin_clzll(lo) : 0);
+                bits[l] = std::max(bits[l], b);
+            }
+        }
+        it = cache.emplace(ell, std::move(bits)).first;
+    }
+    return it->second[layer];
 }
 
 uint32_t default_schedule(const Shape &s) {
@@ -277,6 +312,172 @@ __global__ void __launch_bounds__(THREADS, MINB) ntt_table_pass2_pf(TablePassArg
         if (!tz[1]) v[0] = gf_add(v[0], lane_ctx.mul(T1, v[1]));
         v[1] = gf_add(v[1], v[0]);
         if (!tz[2]) v[2] = gf_add(v[2], lane_ctx.mul(T2, v[3]));
+        v[3] = gf_add(v[3], v[2]);
+        const uint64_t rr = (task >> a.log_lanes) & q_mask;
+        const uint64_t ln = task & lanes_mask;
+#pragma unroll
+        for (int g = 0; g < 4; ++g) {
+            const uint64_t p = (B << (log_q + 2)) + ((uint64_t)g << log_q) + rr;
+            __stcs(a.dst + ((p << a.log_lanes) | ln), v[g]);
+        }
+    }
+}
+
+// ---- Compact tables for narrow twiddles ------------------------------------
+// The deepest layers have narrow twiddles (about ell, 2 ell - 3, 4 ell - 11
+// bits at depths 0, 1, 2).  For a twiddle t of w bits, a byte x multiplies
+// into u[x] = x (x) t, an unreduced carry-less product of w + 7 bits, so one
+// 256-entry table of W words (W = 1 for w <= 25, W = 2 for w <= 57) serves
+// all 16 byte positions: t * v = reduce(XOR_k u[v_k] << 8k), each shift fixed
+// per k.  The table is stored in bank copies (W = 1: 32 copies of 4 B, word
+// x * 32 + c; W = 2: 16 copies of 8 B, slot x * 16 + c) and a thread reads
+// the copy of its lane, so the lookups of a warp (W = 1) or half-warp (W = 2)
+// always hit distinct banks: one wavefront per 32 lookups for W = 1, two for
+// W = 2, against four for the 16-byte entries of a byte table; the shifts
+// cost a few more ALU operations.  Every compact table is 32 KB.
+constexpr int kNwBytes = 32768;
+
+constexpr int narrow_class(int bits) { return bits + 7 <= 32 ? 1 : (bits + 7 <= 64 ? 2 : 4); }
+
+// Build the compact table of t (W words wide) into tb; all threads.  Thread
+// pair (x, h) writes half of x's copies, rotated by x, so that every store
+// instruction of a warp covers the banks once.
+template <int W>
+__device__ __forceinline__ void nw_build(char *tb, uint64_t t) {
+    constexpr int copies = W == 1 ? 32 : 16, half = copies / 2;
+    for (int u = threadIdx.x; u < 512; u += blockDim.x) {
+        const uint32_t x = (uint32_t)u >> 1, h = (uint32_t)u & 1;
+        uint64_t p = 0;
+#pragma unroll
+        for (int i = 0; i < 8; ++i)
+            if ((x >> i) & 1) p ^= t << i;
+#pragma unroll
+        for (int i = 0; i < half; ++i) {
+            const uint32_t c = h * half + ((i + x) & (half - 1));
+            if (W == 1)
+                reinterpret_cast<uint32_t *>(tb)[x * 32 + c] = (uint32_t)p;
+            else
+                reinterpret_cast<uint2 *>(tb)[x * 16 + c] =
+                    make_uint2((uint32_t)p, (uint32_t)(p >> 32));
+        }
+    }
+}
+
+// t * v through the compact table tb of width W.
+template <int W>
+__device__ __forceinline__ uint4 nw_mul(const char *tb, uint4 v) {
+    const uint32_t lane_off = W == 1 ? (threadIdx.x & 31) << 2 : (threadIdx.x & 15) << 3;
+    const uint32_t w[4] = {v.x, v.y, v.z, v.w};
+    uint32_t acc[6] = {0, 0, 0, 0, 0, 0};
+#pragma unroll
+    for (int q = 0; q < 4; ++q) {
+#pragma unroll
+        for (int r = 0; r < 4; ++r) {
+            // byte r of word q, times 128 (the row pitch of both layouts)
+            const uint32_t x7 = (r == 0 ? (w[q] << 7) : (w[q] >> (8 * r - 7))) & 0x7F80u;
+            if (W == 1) {
+                const uint32_t u = *reinterpret_cast<const uint32_t *>(tb + (x7 | lane_off));
+                acc[q] ^= u << (8 * r);
+                if (r) acc[q + 1] ^= u >> (32 - 8 * r);
+            } else {
+                const uint2 u = *reinterpret_cast<const uint2 *>(tb + (x7 | lane_off));
+                if (r == 0) {
+                    acc[q] ^= u.x;
+                    acc[q + 1] ^= u.y;
+                } else {
+                    acc[q] ^= u.x << (8 * r);
+                    acc[q + 1] ^= __funnelshift_l(u.x, u.y, 8 * r);
+                    acc[q + 2] ^= u.y >> (32 - 8 * r);
+                }
+            }
+        }
+    }
+    // bits 128 and up: X^128 = X^7 + X^2 + X + 1
+    const uint64_t h = (uint64_t)acc[4] | ((uint64_t)acc[5] << 32);
+    const uint64_t f = h ^ (h << 1) ^ (h << 2) ^ (h << 7);
+    // h < 2^56 (products of at most 64 bits shifted by at most 120), so f
+    // stays below 2^63 and needs no second fold
+    return make_uint4(acc[0] ^ (uint32_t)f, acc[1] ^ (uint32_t)(f >> 32), acc[2], acc[3]);
+}
+
+// Radix-4 pass whose second-layer twiddles t_a, t_b are narrow (compact
+// tables of width WAB) and whose t_o uses a compact table of width WO, or
+// its 64 KB byte table when WO == 4.  Loads of the next task in flight, as
+// in ntt_table_pass2_pf.
+template <int WO, int WAB>
+__global__ void __launch_bounds__(512, 1) ntt_table_pass2_nw(TablePassArgs a) {
+    constexpr bool FULL_O = WO == 4;
+    extern __shared__ uint4 smem[];
+    uint4 *tbl = smem;  // t_o byte table (FULL_O)
+    uint4 *bases = smem + (FULL_O ? kT16Entries : 0);
+    char *cw = reinterpret_cast<char *>(smem + (FULL_O ? kT16Entries + kT16Bases : 0));
+    char *cw_a = cw, *cw_b = cw + kNwBytes, *cw_o = cw + 2 * kNwBytes;
+    __shared__ uint4 tw_buf[kTwWindow * 3];
+    __shared__ uint64_t win[2];
+    __shared__ int tz[3];
+    if (threadIdx.x == 0) win[0] = win[1] = 0;
+    T16Lane8 lane_ctx;
+    if (FULL_O) lane_ctx.init();
+    const int log_q = a.ell - a.layer - 2;
+    const int log_task_per_b = log_q + a.log_lanes;
+    const uint64_t lanes_mask = ((uint64_t)1 << a.log_lanes) - 1;
+    const uint64_t q_mask = ((uint64_t)1 << log_q) - 1;
+    const uint64_t src_mask = ((uint64_t)1 << a.src_pos_bits) - 1;
+    const uint64_t chunks = a.n_tasks / blockDim.x;
+    const uint64_t c_beg = chunks * blockIdx.x / gridDim.x;
+    const uint64_t c_end = chunks * (blockIdx.x + 1) / gridDim.x;
+    const uint64_t b_last = (a.task_base + c_end * blockDim.x - 1) >> log_task_per_b;
+    int64_t cur_b = -1;
+    auto src_index = [&](uint64_t task, int g) -> uint64_t {
+        const uint64_t B = task >> log_task_per_b;
+        const uint64_t rr = (task >> a.log_lanes) & q_mask;
+        const uint64_t p = (B << (log_q + 2)) + ((uint64_t)g << log_q) + rr;
+        return ((p & src_mask) << a.log_lanes) | (task & lanes_mask);
+    };
+    auto lo64 = [](uint4 t) { return (uint64_t)t.x | ((uint64_t)t.y << 32); };
+    uint4 nxt[4];
+    if (c_beg < c_end) {
+        const uint64_t t0 = a.task_base + c_beg * blockDim.x + threadIdx.x;
+#pragma unroll
+        for (int g = 0; g < 4; ++g) nxt[g] = __ldcs(a.src + src_index(t0, g));
+    }
+    for (uint64_t c = c_beg; c < c_end; ++c) {
+        const uint64_t task = a.task_base + c * blockDim.x + threadIdx.x;
+        const uint64_t B = task >> log_task_per_b;  // uniform across the CTA
+        uint4 v[4];
+#pragma unroll
+        for (int g = 0; g < 4; ++g) v[g] = nxt[g];
+        if (c + 1 < c_end) {
+            const uint64_t tn = task + blockDim.x;
+#pragma unroll
+            for (int g = 0; g < 4; ++g) nxt[g] = __ldcs(a.src + src_index(tn, g));
+        }
+        if ((int64_t)B != cur_b) {
+            __syncthreads();
+            const uint4 *ts = tw_window<3>(a.tw, a.layer, B, b_last, tw_buf, win);
+            if (threadIdx.x < 3) tz[threadIdx.x] = gf_is_zero(ts[threadIdx.x]);
+            if constexpr (FULL_O) t16_build(tbl, bases, ts, 1);
+            else nw_build<WO>(cw_o, lo64(ts[0]));
+            nw_build<WAB>(cw_a, lo64(ts[1]));
+            nw_build<WAB>(cw_b, lo64(ts[2]));
+            __syncthreads();
+            cur_b = (int64_t)B;
+        }
+        if (!tz[0]) {
+            if constexpr (FULL_O) {
+                const char *T0 = reinterpret_cast<const char *>(tbl);
+                v[0] = gf_add(v[0], lane_ctx.mul(T0, v[2]));
+                v[1] = gf_add(v[1], lane_ctx.mul(T0, v[3]));
+            } else {
+                v[0] = gf_add(v[0], nw_mul<WO>(cw_o, v[2]));
+                v[1] = gf_add(v[1], nw_mul<WO>(cw_o, v[3]));
+            }
+        }
+        v[2] = gf_add(v[2], v[0]);
+        v[3] = gf_add(v[3], v[1]);
+        if (!tz[1]) v[0] = gf_add(v[0], nw_mul<WAB>(cw_a, v[1]));
+        v[1] = gf_add(v[1], v[0]);
+        if (!tz[2]) v[2] = gf_add(v[2], nw_mul<WAB>(cw_b, v[3]));
         v[3] = gf_add(v[3], v[2]);
         const uint64_t rr = (task >> a.log_lanes) & q_mask;
         const uint64_t ln = task & lanes_mask;
@@ -485,6 +686,11 @@ static size_t table_smem(int layers) {
     return (size_t)nt * kT16Entries * 16 + (size_t)nt * kT16Bases * 16;
 }
 
+static size_t narrow_smem(bool full_o) {
+    return full_o ? (size_t)(kT16Entries + kT16Bases) * 16 + (size_t)2 * kNwBytes
+                  : (size_t)3 * kNwBytes;
+}
+
 #define BZ_TAIL_ATTR(DT, DN, M)                                                           \
     cudaFuncSetAttribute(ntt_tail_pass<DT, DN, M>, cudaFuncAttributeMaxDynamicSharedMemorySize, \
                          (int)table_smem(DT))
@@ -505,6 +711,15 @@ void init_ntt_kernels() {
                          (int)table_smem(2));
     cudaFuncSetAttribute(ntt_table_pass<1, 256>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                          (int)table_smem(1));
+#define BZ_NW_ATTR(WO, WAB)                                                               \
+    cudaFuncSetAttribute(ntt_table_pass2_nw<WO, WAB>,                                       \
+                         cudaFuncAttributeMaxDynamicSharedMemorySize, (int)narrow_smem(WO == 4))
+    BZ_NW_ATTR(1, 1);
+    BZ_NW_ATTR(2, 1);
+    BZ_NW_ATTR(4, 1);
+    BZ_NW_ATTR(2, 2);
+    BZ_NW_ATTR(4, 2);
+#undef BZ_NW_ATTR
     BZ_TAIL_ATTR_M(1, 1); BZ_TAIL_ATTR_M(1, 2); BZ_TAIL_ATTR_M(1, 3);
     BZ_TAIL_ATTR_M(2, 1); BZ_TAIL_ATTR_M(2, 2);
 }
@@ -524,9 +739,17 @@ static void launch_tail(const DeepArgs &a, int mode, unsigned grid, cudaStream_t
     else ntt_tail_pass<DT, DN, 0><<<grid, 512, sm, st>>>(a);
 }
 
+// Whether a table pass runs as ntt_table_pass2_nw (compact tables for the
+// narrow twiddles of its second layer, and of its first when narrow too).
+bool narrow_table_pass(const Shape &s, uint32_t schedule, int layer, int layers, int threads) {
+    return (schedule & SCHED_NARROW) && layers == 2 && threads == 512 &&
+           narrow_class(twiddle_bits(s.k_code(), layer + 1)) <= 2;
+}
+
 int launch_table_pass(const Shape &s, int layer, int layers, const uint4 *src, int src_bits,
                       uint4 *dst, const uint4 *tw, uint64_t p0, uint64_t p1, int threads,
-                      cudaStream_t st, int num_sms, bool prefetch, bool lean) {
+                      cudaStream_t st, int num_sms, uint32_t schedule) {
+    const bool prefetch = (schedule & SCHED_PREFETCH) != 0, lean = (schedule & SCHED_LEAN) != 0;
     const int ell = s.k_code(), L = s.log_lanes;
     const int log_q = ell - layer - layers;  // quad / pair stride (positions)
     TablePassArgs a;
@@ -543,7 +766,16 @@ int launch_table_pass(const Shape &s, int layer, int layers, const uint4 *src, i
     a.n_tasks = ((b1 - b0) << log_q) << L;
     const unsigned grid =
         (unsigned)std::max<uint64_t>(1, std::min<uint64_t>(num_sms, a.n_tasks / threads));
-    if (prefetch && layers == 2) {
+    if (narrow_table_pass(s, schedule, layer, layers, threads)) {
+        const int wo = narrow_class(twiddle_bits(ell, layer));
+        const int wab = narrow_class(twiddle_bits(ell, layer + 1));
+        const size_t sm = narrow_smem(wo == 4);
+        if (wab == 1 && wo == 1) ntt_table_pass2_nw<1, 1><<<grid, 512, sm, st>>>(a);
+        else if (wab == 1 && wo == 2) ntt_table_pass2_nw<2, 1><<<grid, 512, sm, st>>>(a);
+        else if (wab == 1) ntt_table_pass2_nw<4, 1><<<grid, 512, sm, st>>>(a);
+        else if (wo == 2) ntt_table_pass2_nw<2, 2><<<grid, 512, sm, st>>>(a);
+        else ntt_table_pass2_nw<4, 2><<<grid, 512, sm, st>>>(a);
+    } else if (prefetch && layers == 2) {
         if (threads == 256 && lean)
             ntt_table_pass2_pf<256, 2><<<grid, 256, table_smem(2), st>>>(a);
         else if (threads == 256)
@@ -642,13 +874,13 @@ int launch_ntt(const Shape &s, uint32_t schedule, const uint4 *d_msg, uint4 *d_c
             continue;
         }
         launches += launch_table_pass(s, layer, layers, src, src_bits, d_cw, d_tw, 0, P, threads,
-                                      st, num_sms, (schedule & SCHED_PREFETCH) != 0,
-                                      (schedule & SCHED_LEAN) != 0);
+                                      st, num_sms, schedule);
         if (log) {
             // "<kernel>@<first layer>": the profile's reader counts the
             // multiplies of each launch from its layer
-            std::string n = layers == 2 ? (src == d_msg ? "ntt_table_pass2_first" : "ntt_table_pass2")
-                                        : (src == d_msg ? "ntt_table_pass1_first" : "ntt_table_pass1");
+            std::string n = layers == 2 ? "ntt_table_pass2" : "ntt_table_pass1";
+            if (src == d_msg) n += "_first";
+            if (narrow_table_pass(s, schedule, layer, layers, threads)) n += "_nw";
             log->mark((n + "@" + std::to_string(layer)).c_str());
         }
         src = d_cw;

@@ -44,9 +44,8 @@ int launch_commit_pipelined(const Shape &s, uint32_t schedule, const uint4 *d_ms
         layer += layers;
     }
     const uint64_t P = (uint64_t)1 << ell;
-    const bool pf = (schedule & SCHED_PREFETCH) != 0, lean = (schedule & SCHED_LEAN) != 0;
     int launches =
-        launch_table_pass(s, r, first, d_msg, b, d_cw, d_tw, 0, P, threads, st, num_sms, pf, lean);
+        launch_table_pass(s, r, first, d_msg, b, d_cw, d_tw, 0, P, threads, st, num_sms, schedule);
     if (log)
         log->mark((std::string(first == 2 ? "ntt_table_pass2_first" : "ntt_table_pass1_first") +
                    "@" + std::to_string(r))
@@ -56,7 +55,7 @@ int launch_commit_pipelined(const Shape &s, uint32_t schedule, const uint4 *d_ms
         for (int layer = r + first; layer < table_end;) {
             const int layers = (!radix2 && layer + 1 < table_end) ? 2 : 1;
             launches += launch_table_pass(s, layer, layers, d_cw, 62, d_cw, d_tw, p0, p1, threads,
-                                          st, num_sms, pf, lean);
+                                          st, num_sms, schedule);
             layer += layers;
         }
         cudaEventRecord(ev[k], st);

@@ -66,7 +66,8 @@ SCHEDULES = [0, 1, 2, 3, 4, 0x10, 0x13, 0x20,
              0x200 | 2, (1 << 10) | 2, (2 << 10) | 0x200 | 2, (3 << 10) | 0x200 | 2,
              (2 << 10) | 0x200 | 3 | (1 << 7), (1 << 10) | 0x10 | 2, (3 << 10) | 0x200 | 0x11,
              0x1000 | 2, 0x1200 | 2, 0x1000 | (1 << 10) | 2, 0x1000 | 0, 0x3602, 0x3a03,
-             (1 << 10), (2 << 10) | 0x200, (3 << 10) | 0x3200, 0x1200 | (1 << 10), 0x3200]
+             (1 << 10), (2 << 10) | 0x200, (3 << 10) | 0x3200, 0x1200 | (1 << 10), 0x3200,
+             0x4000, 0x5000, 0x5400, 0x5C00, 0x5001, 0x5002, 0x4010]
 
 
 @pytest.mark.parametrize("schedule", SCHEDULES)
@@ -100,6 +101,47 @@ def test_roots_fixture(ctx):
         pd.free()
         msg.free()
         assert c.root.hex() == e["root"], e
+
+
+@pytest.mark.parametrize("schedule", [0x5000, 0x5400, 0x5001])
+def test_compact_twiddle_tables_at_benchmark_shapes(ctx, schedule):
+    """Compact tables for the narrow twiddles of the deepest radix-4 pass
+    (all three twiddles at 2^20 and 2^24, the second layer's only at 2^28
+    shapes), against the committed oracle roots of the benchmark shapes."""
+    from bitz_gb300 import DeviceArray, PcsParams, commit
+
+    with open(os.path.join(GOLDEN, "roots.json")) as fh:
+        roots = json.load(fh)["roots"]
+    for e in roots:
+        if e["log_msg_len"] not in (20, 24, 28) or e["hash"] != "blake3":
+            continue
+        p = PcsParams(e["log_msg_len"] + 7, e["log_inv_rate"], e["log_batch_size"], 1)
+        ctx.set_schedule(p, schedule)
+        msg = DeviceArray.chacha(e["seed"], 1 << e["log_msg_len"], ctx)
+        try:
+            c, pd = commit(msg, p, ctx)
+            pd.free()
+            assert c.root.hex() == e["root"], (hex(schedule), e)
+        finally:
+            msg.free()
+            ctx.set_schedule(p, 3)
+
+
+@pytest.mark.parametrize("schedule", [0x5000, 0x5400])
+def test_compact_twiddle_tables_two_word(oracle, ctx, schedule):
+    """2^22 words at rate 1/8 (ell = 16, passes from layer 3): the pass at
+    layer 13 has t_o of 53 bits and t_a, t_b of 29 bits, both in two-word
+    compact tables; the codeword root must equal the oracle's."""
+    from bitz_gb300 import PcsParams
+
+    msg = oracle.chacha_words(5, 1 << 22)
+    _, _, root = oracle.commit(msg, 3, 9, 1, n_threads=16)
+    try:
+        c, pd = _gpu_commit(msg, 3, 9, 1, ctx, schedule)
+        pd.free()
+        assert c.root == root
+    finally:
+        ctx.set_schedule(PcsParams(22 + 7, 3, 9, 1), 3)
 
 
 def test_cmt1_fixture(ctx):
