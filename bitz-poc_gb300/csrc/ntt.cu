@@ -22,11 +22,14 @@
 //     the 8 threads of a quarter-warp always hit 8 different bank groups, so
 //     the 128-bit lookups are bank-conflict free.  The first table pass reads
 //     the message and writes all 2^r replicas (the replicate fill is fused).
+//   * the deepest radix-4 passes (schedule bit SCHED_NARROW) exploit that
+//     their twiddles are narrow (at depth i the twiddle has at most about
+//     2^i * ell bits): a byte times such a twiddle is an unreduced product of
+//     at most 64 bits, so one compact 256-entry table of one or two words
+//     replaces the sixteen 16-byte tables (ntt_table_pass2_nw).
 //   * the "deep" pass runs the last D layers (D <= 4) on 2^D consecutive
-//     positions held in registers.  Their twiddles are narrow (at depth i the
-//     twiddle has at most ~2^i * ell bits: x^(j+1) at the deepest layer), so
-//     the multiply is a shift-and-XOR over the twiddle's set bits, with the
-//     twiddle warp-uniform.
+//     positions held in registers, the multiply being a shift-and-XOR over
+//     the narrow twiddle's set bits, with the twiddle warp-uniform.
 #include <cuda_runtime.h>
 
 #include <algorithm>
