@@ -3,7 +3,9 @@
 ``Server.submit_commit`` queues a commit of a host message; the native
 scheduler admits it when an execution slot and device memory are free.
 ``submit_open`` queues the opening (rows + multi-proof) of a committed
-request, after which its resident codeword and tree are freed.
+request, after which its resident codeword and tree are freed;
+``submit_commit_open`` queues both at once.  ``next_done`` is the completion
+queue: the ids of requests whose state changed, without polling each one.
 """
 from __future__ import annotations
 
@@ -24,7 +26,10 @@ _SIGS = {
     "bz_server_create": (ctypes.c_int, [_P, ctypes.c_int, _U64, _S, ctypes.POINTER(_P)]),
     "bz_server_submit_commit": (ctypes.c_int, [_P, _P, _S, ctypes.POINTER(Params),
                                                ctypes.POINTER(_U64)]),
+    "bz_server_submit_commit_open": (ctypes.c_int, [_P, _P, _S, ctypes.POINTER(Params), _P, _S,
+                                                    ctypes.POINTER(_U64)]),
     "bz_server_submit_open": (ctypes.c_int, [_P, _U64, _P, _S]),
+    "bz_server_next_done": (ctypes.c_int, [_P, _P, _P, _S, ctypes.POINTER(_S), ctypes.c_uint32]),
     "bz_server_poll": (ctypes.c_int, [_P, _U64, ctypes.POINTER(ctypes.c_int)]),
     "bz_server_wait": (ctypes.c_int, [_P, _U64, ctypes.c_int, ctypes.c_uint32]),
     "bz_server_root": (ctypes.c_int, [_P, _U64, _P]),
@@ -87,6 +92,32 @@ class Server:
         check(self.ctx.handle, self.L.bz_server_submit_commit(self.h, host_ptr, n_words,
                                                               ctypes.byref(p), ctypes.byref(rid)))
         return rid.value
+
+    def submit_commit_open(self, msg: np.ndarray, params: PcsParams, positions) -> int:
+        msg = np.ascontiguousarray(msg, dtype=np.uint64).reshape(-1, 2)
+        rid = self.submit_commit_open_ptr(msg.ctypes.data, msg.shape[0], params, positions)
+        self._keep[rid] = msg
+        return rid
+
+    def submit_commit_open_ptr(self, host_ptr: int, n_words: int, params: PcsParams,
+                               positions) -> int:
+        p = params.to_c()
+        pos = np.ascontiguousarray(np.asarray(positions, dtype=np.uint64))
+        rid = _U64()
+        check(self.ctx.handle, self.L.bz_server_submit_commit_open(
+            self.h, host_ptr, n_words, ctypes.byref(p), ptr(pos) if len(pos) else None, len(pos),
+            ctypes.byref(rid)))
+        return rid.value
+
+    def next_done(self, cap: int = 64, timeout_us: int = 0) -> list[tuple[int, int]]:
+        """(id, state entered) for the state changes since the previous call
+        (bounded wait)."""
+        ids = np.zeros(max(cap, 1), np.uint64)
+        states = np.zeros(max(cap, 1), np.int32)
+        n = _S()
+        check(self.ctx.handle, self.L.bz_server_next_done(self.h, ptr(ids), ptr(states), cap,
+                                                          ctypes.byref(n), int(timeout_us)))
+        return [(int(i), int(st)) for i, st in zip(ids[:n.value], states[:n.value])]
 
     def submit_open(self, rid: int, positions) -> None:
         pos = np.ascontiguousarray(np.asarray(positions, dtype=np.uint64))

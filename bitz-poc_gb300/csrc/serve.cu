@@ -14,6 +14,14 @@
 // The server uses its own streams and its own scratch-free shapes (leaves up
 // to 256 BLAKE3 chunks); while it runs, the owning context may still be used
 // from other threads for unrelated work on the context stream.
+//
+// Nothing on the request path synchronises the device: device buffers come
+// from the stream-ordered pool (cudaMallocAsync / cudaFreeAsync on the slot's
+// stream), and each slot owns its completion event and a grow-only pinned
+// staging buffer for the root, rows and proof nodes, which the scheduler
+// copies into the request when the slot's work completes.  A completion
+// queue (bz_server_next_done) hands state changes to the caller without
+// polling every request.
 #include <cuda_runtime.h>
 
 #include <chrono>
@@ -55,17 +63,13 @@ struct Request {
     uint4 *d_msg = nullptr;
     bz_commitment *commit = nullptr;
     int slot = -1;
-    cudaEvent_t done = nullptr;
     uint8_t root[32] = {0};
-    uint8_t *h_root = nullptr;  // pinned 32 B
     // opening
+    bool auto_open = false;  // queue the opening as soon as the commit is done
     std::vector<uint64_t> positions;
     std::vector<uint64_t> node_idx;
-    uint64_t *d_pos = nullptr, *d_idx = nullptr;
-    uint4 *d_rows = nullptr;
-    uint8_t *d_nodes = nullptr;
-    uint64_t *h_rows = nullptr;   // pinned
-    uint8_t *h_nodes = nullptr;   // pinned
+    std::vector<uint64_t> rows;  // q rows of 2^log_lanes elements
+    std::vector<uint8_t> nodes;  // n_hashes * 32 bytes
     // timestamps (ns since server start)
     int64_t t_submit = 0, t_start = 0, t_committed = 0, t_open_submit = 0, t_opened = 0;
     size_t bytes = 0;
@@ -79,7 +83,12 @@ struct bz_server {
     uint64_t budget = 0, in_use = 0;
     size_t queue_cap = 0;
     std::vector<cudaStream_t> streams;
+    std::vector<cudaEvent_t> slot_done;    // completion of the slot's work
+    std::vector<uint8_t *> slot_host;      // pinned staging (root, rows, nodes)
+    std::vector<size_t> slot_host_bytes;
     std::vector<bool> slot_busy;
+    std::deque<std::pair<uint64_t, int>> completed;  // (id, new state) for bz_server_next_done
+    bool notify = false;                   // completions are recorded once asked for
     std::mutex mu;
     std::condition_variable cv_work, cv_done;
     std::deque<uint64_t> pending_commits, pending_opens;
@@ -101,18 +110,57 @@ size_t request_bytes(const Shape &s) {
     return s.msg_words() * 16 + s.cw_words() * 16 + s.tree_nodes() * 32;
 }
 
-void release_open_buffers(Request *r) {
-    if (r->d_pos) cudaFree(r->d_pos);
-    if (r->d_idx) cudaFree(r->d_idx);
-    if (r->d_rows) cudaFree(r->d_rows);
-    if (r->d_nodes) cudaFree(r->d_nodes);
-    if (r->h_rows) cudaFreeHost(r->h_rows);
-    if (r->h_nodes) cudaFreeHost(r->h_nodes);
-    r->d_pos = r->d_idx = nullptr;
-    r->d_rows = nullptr;
-    r->d_nodes = nullptr;
-    r->h_rows = nullptr;
-    r->h_nodes = nullptr;
+// Multi-proof node indices of sorted unique positions
+// (flock-core/src/merkle.rs:688-741).
+std::vector<uint64_t> multiproof_nodes(std::vector<uint64_t> act, uint64_t n_leaves) {
+    std::vector<uint64_t> idx;
+    uint64_t level_start = 0, level_len = n_leaves;
+    while (level_len > 1 && !act.empty()) {
+        std::vector<uint64_t> next;
+        size_t i = 0;
+        while (i < act.size()) {
+            const uint64_t p = act[i];
+            if (i + 1 < act.size() && act[i + 1] == (p ^ 1)) {
+                i += 2;
+            } else {
+                idx.push_back(level_start + (p ^ 1));
+                i += 1;
+            }
+            next.push_back(p >> 1);
+        }
+        act.swap(next);
+        level_start += level_len;
+        level_len >>= 1;
+    }
+    return idx;
+}
+
+// Sorted unique positions, all below n_leaves (else false).
+bool set_positions(Request *r, const uint64_t *positions, size_t q) {
+    const uint64_t n_leaves = r->shape.n_leaves();
+    std::vector<uint64_t> act(positions, positions + q);
+    for (uint64_t p : act)
+        if (p >= n_leaves) return false;
+    std::sort(act.begin(), act.end());
+    act.erase(std::unique(act.begin(), act.end()), act.end());
+    r->node_idx = multiproof_nodes(act, n_leaves);
+    r->positions = std::move(act);
+    return true;
+}
+
+// Grow slot's pinned staging to `bytes` (the slot is idle when called).
+int ensure_slot_host(bz_server *S, int slot, size_t bytes) {
+    if (S->slot_host_bytes[slot] >= bytes) return BZ_OK;
+    const size_t want = std::max(bytes, (size_t)2 * S->slot_host_bytes[slot]);
+    if (S->slot_host[slot]) cudaFreeHost(S->slot_host[slot]);
+    S->slot_host[slot] = nullptr;
+    S->slot_host_bytes[slot] = 0;
+    if (cudaMallocHost(&S->slot_host[slot], want) != cudaSuccess) {
+        cudaGetLastError();
+        return BZ_ERR_NOMEM;
+    }
+    S->slot_host_bytes[slot] = want;
+    return BZ_OK;
 }
 
 // Start a commit on a free slot (caller holds the lock).
@@ -147,9 +195,9 @@ int start_commit(bz_server *S, Request *r, int slot) {
     ctx->launches += (uint64_t)n;
     cudaFreeAsync(r->d_msg, st);
     r->d_msg = nullptr;
-    cudaMemcpyAsync(r->h_root, c->d_tree + (s.tree_nodes() - 1) * 32, 32, cudaMemcpyDeviceToHost,
-                    st);
-    cudaEventRecord(r->done, st);
+    cudaMemcpyAsync(S->slot_host[slot], c->d_tree + (s.tree_nodes() - 1) * 32, 32,
+                    cudaMemcpyDeviceToHost, st);
+    cudaEventRecord(S->slot_done[slot], st);
     e = cudaGetLastError();
     if (e != cudaSuccess) return BZ_ERR_CUDA;
     return BZ_OK;
@@ -161,24 +209,30 @@ int start_open(bz_server *S, Request *r, int slot) {
     const Shape &s = r->shape;
     const size_t q = r->positions.size(), nn = r->node_idx.size();
     const size_t row_bytes = s.leaf_bytes();
-    if (cudaMalloc(&r->d_pos, (q ? q : 1) * 8) != cudaSuccess ||
-        cudaMalloc(&r->d_idx, (nn ? nn : 1) * 8) != cudaSuccess ||
-        cudaMalloc(&r->d_rows, (q ? q : 1) * row_bytes) != cudaSuccess ||
-        cudaMalloc(&r->d_nodes, (nn ? nn : 1) * 32) != cudaSuccess ||
-        cudaMallocHost(&r->h_rows, (q ? q : 1) * row_bytes) != cudaSuccess ||
-        cudaMallocHost(&r->h_nodes, (nn ? nn : 1) * 32) != cudaSuccess) {
+    // pinned staging: rows then nodes; device: positions, node indices,
+    // rows, nodes in one stream-ordered allocation
+    int rc = ensure_slot_host(S, slot, q * row_bytes + nn * 32 + 32);
+    if (rc) return rc;
+    const size_t o_idx = q * 8, o_rows = (o_idx + nn * 8 + 15) & ~(size_t)15;
+    const size_t o_nodes = o_rows + q * row_bytes, dev_bytes = o_nodes + nn * 32 + 16;
+    uint8_t *d = nullptr;
+    if (cudaMallocAsync((void **)&d, dev_bytes, st) != cudaSuccess) {
         cudaGetLastError();
-        release_open_buffers(r);
         return BZ_ERR_NOMEM;
     }
-    if (q) cudaMemcpyAsync(r->d_pos, r->positions.data(), q * 8, cudaMemcpyHostToDevice, st);
-    if (nn) cudaMemcpyAsync(r->d_idx, r->node_idx.data(), nn * 8, cudaMemcpyHostToDevice, st);
-    int n = launch_gather_rows(r->commit->d_cw, s.log_lanes, r->d_pos, q, r->d_rows, st);
-    n += launch_gather_nodes(r->commit->d_tree, r->d_idx, nn, r->d_nodes, st);
+    uint64_t *d_pos = (uint64_t *)d, *d_idx = (uint64_t *)(d + o_idx);
+    uint4 *d_rows = (uint4 *)(d + o_rows);
+    uint8_t *d_nodes = d + o_nodes;
+    if (q) cudaMemcpyAsync(d_pos, r->positions.data(), q * 8, cudaMemcpyHostToDevice, st);
+    if (nn) cudaMemcpyAsync(d_idx, r->node_idx.data(), nn * 8, cudaMemcpyHostToDevice, st);
+    int n = launch_gather_rows(r->commit->d_cw, s.log_lanes, d_pos, q, d_rows, st);
+    n += launch_gather_nodes(r->commit->d_tree, d_idx, nn, d_nodes, st);
     ctx->launches += (uint64_t)n;
-    if (q) cudaMemcpyAsync(r->h_rows, r->d_rows, q * row_bytes, cudaMemcpyDeviceToHost, st);
-    if (nn) cudaMemcpyAsync(r->h_nodes, r->d_nodes, nn * 32, cudaMemcpyDeviceToHost, st);
-    cudaEventRecord(r->done, st);
+    uint8_t *h = S->slot_host[slot];
+    if (q) cudaMemcpyAsync(h, d_rows, q * row_bytes, cudaMemcpyDeviceToHost, st);
+    if (nn) cudaMemcpyAsync(h + q * row_bytes, d_nodes, nn * 32, cudaMemcpyDeviceToHost, st);
+    cudaFreeAsync(d, st);
+    cudaEventRecord(S->slot_done[slot], st);
     return cudaGetLastError() == cudaSuccess ? BZ_OK : BZ_ERR_CUDA;
 }
 
@@ -206,33 +260,46 @@ void scheduler(bz_server *S) {
         // 1. completions
         for (size_t i = 0; i < S->running.size();) {
             Request *r = S->reqs[S->running[i]].get();
-            cudaError_t q = cudaEventQuery(r->done);
+            cudaError_t q = cudaEventQuery(S->slot_done[r->slot]);
             if (q == cudaErrorNotReady) {
                 ++i;
                 continue;
             }
             progress = true;
             S->slot_busy[r->slot] = false;
+            const uint8_t *h = S->slot_host[r->slot];
             if (q != cudaSuccess) {
                 cudaGetLastError();
                 r->state = RS_FAILED;
                 r->error = BZ_ERR_CUDA;
                 ++S->n_failed;
             } else if (r->state == RS_RUNNING) {
-                memcpy(r->root, r->h_root, 32);
+                memcpy(r->root, h, 32);
                 r->commit->root_ready = true;
                 memcpy(r->commit->root, r->root, 32);
                 r->state = RS_COMMITTED;
                 r->t_committed = S->ns();
                 S->in_use -= r->shape.msg_words() * 16;  // staging buffer released
                 ++S->n_committed;
+                if (r->auto_open) {
+                    if (S->notify) S->completed.emplace_back(r->id, RS_COMMITTED);
+                    r->state = RS_OPEN_QUEUED;
+                    r->t_open_submit = r->t_committed;
+                    S->pending_opens.push_back(r->id);
+                }
             } else if (r->state == RS_OPENING) {
+                const size_t q_rows = r->positions.size(), nn = r->node_idx.size();
+                const size_t row_words = (size_t)2 << r->shape.log_lanes;
+                r->rows.assign((const uint64_t *)h, (const uint64_t *)h + q_rows * row_words);
+                r->nodes.assign(h + q_rows * row_words * 8, h + q_rows * row_words * 8 + nn * 32);
                 r->state = RS_OPENED;
                 r->t_opened = S->ns();
                 free_commit_buffers(S, r, r->slot);
                 S->in_use -= r->bytes - r->shape.msg_words() * 16;
                 ++S->n_opened;
             }
+            if (S->notify && !(r->auto_open && r->state == RS_OPEN_QUEUED))
+                S->completed.emplace_back(r->id, r->state);
             S->running[i] = S->running.back();
             S->running.pop_back();
         }
@@ -249,6 +316,8 @@ void scheduler(bz_server *S) {
                 r->state = RS_FAILED;
                 r->error = rc;
                 ++S->n_failed;
+                if (S->notify) S->completed.emplace_back(r->id, r->state);
+                progress = true;
                 continue;
             }
             S->slot_busy[slot] = true;
@@ -272,6 +341,8 @@ void scheduler(bz_server *S) {
                 r->error = rc;
                 S->in_use -= r->bytes;
                 ++S->n_failed;
+                if (S->notify) S->completed.emplace_back(r->id, r->state);
+                progress = true;
                 continue;
             }
             S->slot_busy[slot] = true;
@@ -302,17 +373,37 @@ int bz_server_create(bz_ctx *ctx, int n_slots, uint64_t mem_budget_bytes, size_t
     S->budget = mem_budget_bytes ? mem_budget_bytes : ctx->budget;
     S->queue_cap = queue_cap ? queue_cap : 1 << 20;
     S->streams.resize(n_slots);
+    S->slot_done.resize(n_slots);
+    S->slot_host.assign(n_slots, nullptr);
+    S->slot_host_bytes.assign(n_slots, 0);
     S->slot_busy.assign(n_slots, false);
-    for (auto &s : S->streams) cudaStreamCreateWithFlags(&s, cudaStreamNonBlocking);
+    for (int i = 0; i < n_slots; ++i) {
+        if (cudaStreamCreateWithFlags(&S->streams[i], cudaStreamNonBlocking) != cudaSuccess ||
+            cudaEventCreateWithFlags(&S->slot_done[i], cudaEventDisableTiming) != cudaSuccess ||
+            ensure_slot_host(S, i, 64 << 10) != BZ_OK) {
+            cudaGetLastError();
+            for (int j = 0; j <= i; ++j) {
+                if (S->streams[j]) cudaStreamDestroy(S->streams[j]);
+                if (S->slot_done[j]) cudaEventDestroy(S->slot_done[j]);
+                if (S->slot_host[j]) cudaFreeHost(S->slot_host[j]);
+            }
+            delete S;
+            return BZ_ERR_CUDA;
+        }
+    }
     S->t0 = Clock::now();
     S->thr = std::thread(scheduler, S);
     *out = S;
     return BZ_OK;
 }
 
-int bz_server_submit_commit(bz_server *S, const uint64_t *host_msg, size_t n_words,
-                            const bz_params *params, uint64_t *request_id) {
-    if (!S || !host_msg || !request_id) return BZ_ERR_ARG;
+}  // extern "C"
+
+namespace {
+
+int submit(bz_server *S, const uint64_t *host_msg, size_t n_words, const bz_params *params,
+           const uint64_t *positions, size_t q, bool auto_open, uint64_t *request_id) {
+    if (!S || !host_msg || !request_id || (auto_open && q && !positions)) return BZ_ERR_ARG;
     Shape s;
     std::string why;
     int rc = shape_from_params(params, s, n_words, why);
@@ -323,15 +414,12 @@ int bz_server_submit_commit(bz_server *S, const uint64_t *host_msg, size_t n_wor
     r->host_msg = host_msg;
     r->bytes = request_bytes(s);
     if (r->bytes > S->budget) return set_msg(S->ctx, BZ_ERR_NOMEM, "request exceeds the budget");
-    if (cudaEventCreateWithFlags(&r->done, cudaEventDisableTiming) != cudaSuccess ||
-        cudaMallocHost(&r->h_root, 32) != cudaSuccess)
-        return BZ_ERR_CUDA;
-    std::lock_guard<std::mutex> g(S->mu);
-    if (S->pending_commits.size() >= S->queue_cap) {
-        cudaEventDestroy(r->done);
-        cudaFreeHost(r->h_root);
-        return BZ_ERR_BUSY;
+    if (auto_open) {
+        if (!set_positions(r.get(), positions, q)) return BZ_ERR_ARG;
+        r->auto_open = true;
     }
+    std::lock_guard<std::mutex> g(S->mu);
+    if (S->pending_commits.size() >= S->queue_cap) return BZ_ERR_BUSY;
     r->id = S->next_id++;
     r->t_submit = S->ns();
     *request_id = r->id;
@@ -341,6 +429,21 @@ int bz_server_submit_commit(bz_server *S, const uint64_t *host_msg, size_t n_wor
     return BZ_OK;
 }
 
+}  // namespace
+
+extern "C" {
+
+int bz_server_submit_commit(bz_server *S, const uint64_t *host_msg, size_t n_words,
+                            const bz_params *params, uint64_t *request_id) {
+    return submit(S, host_msg, n_words, params, nullptr, 0, false, request_id);
+}
+
+int bz_server_submit_commit_open(bz_server *S, const uint64_t *host_msg, size_t n_words,
+                                 const bz_params *params, const uint64_t *positions, size_t q,
+                                 uint64_t *request_id) {
+    return submit(S, host_msg, n_words, params, positions, q, true, request_id);
+}
+
 int bz_server_submit_open(bz_server *S, uint64_t id, const uint64_t *positions, size_t q) {
     if (!S || (q && !positions)) return BZ_ERR_ARG;
     std::lock_guard<std::mutex> g(S->mu);
@@ -348,37 +451,28 @@ int bz_server_submit_open(bz_server *S, uint64_t id, const uint64_t *positions, 
     if (it == S->reqs.end()) return BZ_ERR_NOTFOUND;
     Request *r = it->second.get();
     if (r->state != RS_COMMITTED) return BZ_ERR_STATE;
-    const uint64_t n_leaves = r->shape.n_leaves();
-    std::vector<uint64_t> act(positions, positions + q);
-    for (uint64_t p : act)
-        if (p >= n_leaves) return BZ_ERR_ARG;
-    std::sort(act.begin(), act.end());
-    act.erase(std::unique(act.begin(), act.end()), act.end());
-    r->positions = act;
-    // multi-proof node indices (flock-core/src/merkle.rs:688-741)
-    r->node_idx.clear();
-    uint64_t level_start = 0, level_len = n_leaves;
-    while (level_len > 1 && !act.empty()) {
-        std::vector<uint64_t> next;
-        size_t i = 0;
-        while (i < act.size()) {
-            const uint64_t p = act[i];
-            if (i + 1 < act.size() && act[i + 1] == (p ^ 1)) {
-                i += 2;
-            } else {
-                r->node_idx.push_back(level_start + (p ^ 1));
-                i += 1;
-            }
-            next.push_back(p >> 1);
-        }
-        act.swap(next);
-        level_start += level_len;
-        level_len >>= 1;
-    }
+    if (!set_positions(r, positions, q)) return BZ_ERR_ARG;
     r->state = RS_OPEN_QUEUED;
     r->t_open_submit = S->ns();
     S->pending_opens.push_back(id);
     S->cv_work.notify_one();
+    return BZ_OK;
+}
+
+int bz_server_next_done(bz_server *S, uint64_t *ids, int *states, size_t cap, size_t *n,
+                        uint32_t timeout_us) {
+    if (!S || !n || (cap && (!ids || !states))) return BZ_ERR_ARG;
+    std::unique_lock<std::mutex> lk(S->mu);
+    S->notify = true;
+    *n = 0;
+    if (S->completed.empty() && timeout_us)
+        S->cv_done.wait_for(lk, std::chrono::microseconds(timeout_us),
+                            [&] { return !S->completed.empty(); });
+    while (*n < cap && !S->completed.empty()) {
+        ids[*n] = S->completed.front().first;
+        states[(*n)++] = S->completed.front().second;
+        S->completed.pop_front();
+    }
     return BZ_OK;
 }
 
@@ -428,11 +522,11 @@ int bz_server_open_result(bz_server *S, uint64_t id, uint64_t *rows, size_t rows
     if (n_hashes) *n_hashes = nn;
     if (rows) {
         if (rows_cap_words < q * row_words) return BZ_ERR_ARG;
-        memcpy(rows, r->h_rows, q * row_words * 8);
+        if (q) memcpy(rows, r->rows.data(), q * row_words * 8);
     }
     if (proof) {
         if (proof_cap < nn) return BZ_ERR_ARG;
-        memcpy(proof, r->h_nodes, nn * 32);
+        if (nn) memcpy(proof, r->nodes.data(), nn * 32);
     }
     return BZ_OK;
 }
@@ -461,13 +555,10 @@ int bz_server_release(bz_server *S, uint64_t id) {
     if (it == S->reqs.end()) return BZ_ERR_NOTFOUND;
     Request *r = it->second.get();
     if (r->state != RS_OPENED && r->state != RS_FAILED) return BZ_ERR_STATE;
-    release_open_buffers(r);
     if (r->state == RS_FAILED && r->commit) {
         free_commit_buffers(S, r, r->slot);
         S->in_use -= r->bytes - r->shape.msg_words() * 16;
     }
-    if (r->done) cudaEventDestroy(r->done);
-    if (r->h_root) cudaFreeHost(r->h_root);
     S->reqs.erase(it);
     return BZ_OK;
 }
@@ -495,14 +586,15 @@ int bz_server_destroy(bz_server *S) {
     for (auto s : S->streams) cudaStreamSynchronize(s);
     for (auto &kv : S->reqs) {
         Request *r = kv.second.get();
-        release_open_buffers(r);
         if (r->commit) free_commit_buffers(S, r, 0);
-        if (r->done) cudaEventDestroy(r->done);
-        if (r->h_root) cudaFreeHost(r->h_root);
     }
     for (auto s : S->streams) {
         cudaStreamSynchronize(s);
         cudaStreamDestroy(s);
+    }
+    for (int i = 0; i < S->n_slots; ++i) {
+        cudaEventDestroy(S->slot_done[i]);
+        cudaFreeHost(S->slot_host[i]);
     }
     delete S;
     return BZ_OK;

@@ -204,6 +204,12 @@ int bz_server_create(bz_ctx *ctx, int n_slots, uint64_t mem_budget_bytes, size_t
  * holds queue_cap commits. */
 int bz_server_submit_commit(bz_server *s, const uint64_t *host_msg, size_t n_words,
                             const bz_params *params, uint64_t *request_id);
+/* Commit-then-open as one request: the opening at the q positions is queued
+ * as soon as the commit completes (same results as submit_commit followed by
+ * submit_open).  BZ_ERR_ARG for a position outside the codeword. */
+int bz_server_submit_commit_open(bz_server *s, const uint64_t *host_msg, size_t n_words,
+                                 const bz_params *params, const uint64_t *positions, size_t q,
+                                 uint64_t *request_id);
 /* Queue an opening of a committed request at q positions: the opened rows
  * and the multi-proof (merkle_multi_proof order); frees the resident
  * codeword and tree when done. */
@@ -213,6 +219,12 @@ int bz_server_poll(bz_server *s, uint64_t request_id, int *state);
 /* Wait (bounded by timeout_ms) until the request reaches target_state;
  * BZ_ERR_TIMEOUT when the wait runs out. */
 int bz_server_wait(bz_server *s, uint64_t request_id, int target_state, uint32_t timeout_ms);
+/* Completion queue: up to cap state changes since the previous call, in
+ * order, as (ids[i], states[i]) with the state entered (COMMITTED, OPENED or
+ * FAILED); waits up to timeout_us microseconds while none is pending.
+ * Recording starts with the first call. */
+int bz_server_next_done(bz_server *s, uint64_t *ids, int *states, size_t cap, size_t *n,
+                        uint32_t timeout_us);
 int bz_server_root(bz_server *s, uint64_t request_id, uint8_t root[32]);
 /* rows: q * 2^log_batch_size elements for the sorted unique positions;
  * proof: n_hashes * 32 bytes.  Either output may be NULL (size query). */

@@ -51,6 +51,43 @@ def test_server_results_equal_alone_and_in_the_mix(oracle, ctx):
         assert st["in_use"] == 0
 
 
+def test_commit_open_requests_and_completion_queue(oracle, ctx):
+    """submit_commit_open queues the opening itself; the completion queue
+    reports every request's COMMITTED and OPENED, and the results equal the
+    plain path's."""
+    from bitz_gb300 import PcsParams, commit
+    from bitz_gb300.serve import COMMITTED, FAILED, OPENED, Server
+
+    rng = np.random.default_rng(9)
+    shapes = _shapes(rng, 20, 10, 18)
+    msgs = [oracle.chacha_words(900 + i, 1 << k) for i, (k, _) in enumerate(shapes)]
+    params = [PcsParams(k + 7, 2, a, 1) for (k, a) in shapes]
+    qs = [sorted(set(rng.integers(0, p.n_leaves(), 5).tolist())) for p in params]
+    with Server(ctx, n_slots=4) as srv:
+        assert srv.next_done(16, 0) == []
+        ids = [srv.submit_commit_open(m, p, q) for m, p, q in zip(msgs, params, qs)]
+        seen = {rid: [] for rid in ids}
+        opened = 0
+        deadline = time.time() + 120
+        while opened < len(ids) and time.time() < deadline:
+            for rid, st in srv.next_done(64, 100000):
+                assert st != FAILED
+                seen[rid].append(st)
+                opened += st == OPENED
+        assert opened == len(ids)
+        for i, rid in enumerate(ids):
+            assert seen[rid] == [COMMITTED, OPENED]
+            rows, proof = srv.open_result(rid, params[i].num_ntts())
+            c, pd = commit(msgs[i], params[i], ctx)
+            assert srv.root(rid) == c.root
+            assert (rows == pd.rows(qs[i])).all()
+            assert (proof == pd.multi_proof(qs[i])).all()
+            pd.free()
+            srv.release(rid)
+        st = srv.stats()
+        assert st["committed"] == 20 and st["opened"] == 20 and st["in_use"] == 0
+
+
 def test_server_admission_by_memory(oracle, ctx):
     """With a budget that holds one request, the second waits until the first
     is opened (its codeword freed), then runs."""
