@@ -123,7 +123,13 @@ int twiddle_bits(int ell, int layer) {
     return it->second[layer];
 }
 
+// Schedule of a shape the autotuner has not timed.  With at least 512 lanes
+// every layer fits the table passes (each 512-thread chunk stays inside one
+// block), and prefetching radix-4 passes with compact tables for the narrow
+// deep twiddles are what the autotuner picks at 2^20, 2^24 and 2^28; narrower
+// shapes run their last three layers in the register-resident deep pass.
 uint32_t default_schedule(const Shape &s) {
+    if (s.log_lanes >= 9) return SCHED_PREFETCH | SCHED_NARROW;
     const int layers = s.log_dim();
     const int deep = std::min(layers, 3);
     return (uint32_t)deep;
