@@ -110,13 +110,23 @@ int launch_gather_rows(const uint4 *d_cw, int log_lanes, const uint64_t *d_pos, 
 int launch_gather_nodes(const uint8_t *d_tree, const uint64_t *d_idx, size_t n, uint8_t *d_out,
                         cudaStream_t st);
 
-// Folds.  d_partials holds fold_partials_bytes(n) bytes.
+// Folds.  d_partials holds fold_partials_bytes(n) bytes.  With `post`, the
+// last CTA of the fold (or message) kernel reduces the partials itself and
+// posts {u0, u2} to mapped host memory, then the sequence number (no finish
+// kernel, no copy); without it a finish kernel writes d_msg_out.
+struct MsgPost {
+    unsigned int *ticket;  // device counter, 0 between launches
+    uint64_t *words;       // device view of mapped host memory (4 words)
+    uint32_t *seq;         // device view of mapped host memory
+    uint32_t seq_val;
+};
 size_t fold_partials_bytes(size_t n);
 int launch_fold_and_msg(const uint4 *d_f, const uint4 *d_b, size_t n, uint4 r, uint4 *d_nf,
                         uint4 *d_nb, uint64_t *d_partials, uint64_t *d_msg_out, cudaStream_t st,
-                        int num_sms);
+                        int num_sms, const MsgPost *post = nullptr);
 int launch_round_msg(const uint4 *d_f, const uint4 *d_b, size_t n, uint64_t *d_partials,
-                     uint64_t *d_msg_out, cudaStream_t st, int num_sms);
+                     uint64_t *d_msg_out, cudaStream_t st, int num_sms,
+                     const MsgPost *post = nullptr);
 int launch_partial_eval_round(const uint4 *d_in, size_t n, uint4 r, uint4 *d_out,
                               cudaStream_t st);
 int launch_build_eq(const uint4 *d_point_dev, size_t k, uint4 *d_out, cudaStream_t st);

@@ -60,13 +60,80 @@ __device__ __forceinline__ const char *build_r_table(uint4 *smem, uint4 r) {
     return reinterpret_cast<const char *>(smem);
 }
 
+// XOR of the per-CTA partials (8 words each) of n CTAs and the single
+// reduction: out = {u0, u2}.  256 threads: thread t XORs word t mod 8 of
+// partials t / 8, t / 8 + 32, ...; lanes holding the same word then combine
+// by shuffles and across warps.  Partials are read from L2 (other CTAs wrote
+// them in this launch or the previous one).
+constexpr int kFinishThreads = 256;
+__device__ void finish_msg_body(const uint64_t *partials, int n, uint64_t *out) {
+    __shared__ uint64_t red[kFinishThreads / 32][8];
+    __shared__ uint64_t acc[8];
+    const int w = threadIdx.x & 7;
+    uint64_t a = 0;
+    for (int i = threadIdx.x >> 3; i < n; i += kFinishThreads / 8)
+        a ^= __ldcg(partials + (uint64_t)i * 8 + w);
+    a ^= __shfl_xor_sync(0xffffffffu, a, 8);
+    a ^= __shfl_xor_sync(0xffffffffu, a, 16);
+    if ((threadIdx.x & 31) < 8) red[threadIdx.x >> 5][w] = a;
+    __syncthreads();
+    if (threadIdx.x < 8) {
+        uint64_t x = 0;
+        for (int k = 0; k < kFinishThreads / 32; ++k) x ^= red[k][threadIdx.x];
+        acc[threadIdx.x] = x;
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        gf_wide w0, w2;
+        for (int i = 0; i < 4; ++i) {
+            w0.w[i] = acc[i];
+            w2.w[i] = acc[4 + i];
+        }
+        const uint4 u0 = gf_reduce(w0), u2 = gf_reduce(w2);
+        out[0] = lo64(u0);
+        out[1] = hi64(u0);
+        out[2] = lo64(u2);
+        out[3] = hi64(u2);
+    }
+}
+
+// The last CTA of a launch (the one whose ticket completes the count)
+// reduces every CTA's partials and posts {u0, u2} to a mailbox in mapped host
+// memory: the four words, then (after a system-scope fence) the sequence
+// number the host waits for.  It resets the ticket for the next launch.
+// Without a mailbox (ticket null) the caller launches finish_msg_kernel.
+struct MsgMailbox {
+    unsigned int *ticket = nullptr;  // device counter, 0 between launches
+    uint64_t *words = nullptr;       // mapped host memory: u0, u2
+    uint32_t *seq = nullptr;         // mapped host memory
+    uint32_t seq_val = 0;
+};
+
+__device__ void msg_epilogue(const uint64_t *partials, const MsgMailbox &mb) {
+    if (!mb.ticket) return;
+    __shared__ int last;
+    __threadfence();  // this CTA's partial (written before the barrier below)
+    __syncthreads();
+    if (threadIdx.x == 0) last = atomicAdd(mb.ticket, 1u) == gridDim.x - 1;
+    __syncthreads();
+    if (!last) return;
+    __threadfence();
+    finish_msg_body(partials, (int)gridDim.x, mb.words);
+    if (threadIdx.x == 0) {
+        __threadfence_system();
+        *reinterpret_cast<volatile uint32_t *>(mb.seq) = mb.seq_val;
+        *mb.ticket = 0;
+    }
+}
+
 // nf[j] = f[2j] + (f[2j] + f[2j+1]) * r (same for b); thread k produces the
 // folded pair (2k, 2k+1) and its message terms.  The four multiplies by the
 // challenge r use r's byte tables; the two variable products of the message
 // use the generic carry-less multiply.
 __global__ void __launch_bounds__(256) fold_and_msg_kernel(const uint4 *f, const uint4 *b,
                                                            uint64_t half, uint4 r, uint4 *nf,
-                                                           uint4 *nb, uint64_t *partials) {
+                                                           uint4 *nb, uint64_t *partials,
+                                                           MsgMailbox mb) {
     extern __shared__ uint4 smem[];
     const char *T = build_r_table(smem, r);
     T16Lane8 lc;
@@ -94,10 +161,12 @@ __global__ void __launch_bounds__(256) fold_and_msg_kernel(const uint4 *f, const
         nb[0] = gf_add(b[0], gf_mul(gf_add(b[0], b[1]), r));
     }
     cta_store_pair(u0, u2, partials + (uint64_t)blockIdx.x * 8);
+    msg_epilogue(partials, mb);
 }
 
 __global__ void __launch_bounds__(256) round_msg_kernel(const uint4 *f, const uint4 *b,
-                                                        uint64_t pairs, uint64_t *partials) {
+                                                        uint64_t pairs, uint64_t *partials,
+                                                        MsgMailbox mb) {
     gf_wide u0 = gf_wide_zero(), u2 = gf_wide_zero();
     for (uint64_t j = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; j < pairs;
          j += (uint64_t)gridDim.x * blockDim.x) {
@@ -106,42 +175,13 @@ __global__ void __launch_bounds__(256) round_msg_kernel(const uint4 *f, const ui
         gf_wide_xor(u2, gf_mul_wide(gf_add(f0, f1), gf_add(b0, b1)));
     }
     cta_store_pair(u0, u2, partials + (uint64_t)blockIdx.x * 8);
+    msg_epilogue(partials, mb);
 }
 
 // Final XOR of per-CTA partials and the single reduction: out = {u0, u2}.
-// 256 threads: thread t XORs word t mod 8 of partials t / 8, t / 8 + 32, ...;
-// lanes holding the same word then combine by shuffles and across warps.
-constexpr int kFinishThreads = 256;
 __global__ void __launch_bounds__(kFinishThreads) finish_msg_kernel(const uint64_t *partials,
                                                                     int n, uint64_t *out) {
-    __shared__ uint64_t red[kFinishThreads / 32][8];
-    __shared__ uint64_t acc[8];
-    const int w = threadIdx.x & 7;
-    uint64_t a = 0;
-    for (int i = threadIdx.x >> 3; i < n; i += kFinishThreads / 8)
-        a ^= partials[(uint64_t)i * 8 + w];
-    a ^= __shfl_xor_sync(0xffffffffu, a, 8);
-    a ^= __shfl_xor_sync(0xffffffffu, a, 16);
-    if ((threadIdx.x & 31) < 8) red[threadIdx.x >> 5][w] = a;
-    __syncthreads();
-    if (threadIdx.x < 8) {
-        uint64_t x = 0;
-        for (int k = 0; k < kFinishThreads / 32; ++k) x ^= red[k][threadIdx.x];
-        acc[threadIdx.x] = x;
-    }
-    __syncthreads();
-    if (threadIdx.x == 0) {
-        gf_wide w0, w2;
-        for (int i = 0; i < 4; ++i) {
-            w0.w[i] = acc[i];
-            w2.w[i] = acc[4 + i];
-        }
-        const uint4 u0 = gf_reduce(w0), u2 = gf_reduce(w2);
-        out[0] = lo64(u0);
-        out[1] = hi64(u0);
-        out[2] = lo64(u2);
-        out[3] = hi64(u2);
-    }
+    finish_msg_body(partials, n, out);
 }
 
 static int msg_grid(uint64_t work, int num_sms) {
@@ -156,20 +196,26 @@ size_t fold_partials_bytes(size_t n) {
 
 int launch_fold_and_msg(const uint4 *d_f, const uint4 *d_b, size_t n, uint4 r, uint4 *d_nf,
                         uint4 *d_nb, uint64_t *d_partials, uint64_t *d_msg_out, cudaStream_t st,
-                        int num_sms) {
+                        int num_sms, const MsgPost *post) {
     const uint64_t half = n / 2;
     const int grid = std::min(msg_grid(half / 2, num_sms), 1024);
-    fold_and_msg_kernel<<<grid, 256, kRTableSmem, st>>>(d_f, d_b, half, r, d_nf, d_nb,
-                                                         d_partials);
+    MsgMailbox mb;
+    if (post) mb = {post->ticket, post->words, post->seq, post->seq_val};
+    fold_and_msg_kernel<<<grid, 256, kRTableSmem, st>>>(d_f, d_b, half, r, d_nf, d_nb, d_partials,
+                                                         mb);
+    if (post) return 1;
     finish_msg_kernel<<<1, kFinishThreads, 0, st>>>(d_partials, grid, d_msg_out);
     return 2;
 }
 
 int launch_round_msg(const uint4 *d_f, const uint4 *d_b, size_t n, uint64_t *d_partials,
-                     uint64_t *d_msg_out, cudaStream_t st, int num_sms) {
+                     uint64_t *d_msg_out, cudaStream_t st, int num_sms, const MsgPost *post) {
     const uint64_t pairs = n / 2;
     const int grid = std::min(msg_grid(pairs, num_sms), 1024);
-    round_msg_kernel<<<grid, 256, 0, st>>>(d_f, d_b, pairs, d_partials);
+    MsgMailbox mb;
+    if (post) mb = {post->ticket, post->words, post->seq, post->seq_val};
+    round_msg_kernel<<<grid, 256, 0, st>>>(d_f, d_b, pairs, d_partials, mb);
+    if (post) return 1;
     finish_msg_kernel<<<1, kFinishThreads, 0, st>>>(d_partials, grid, d_msg_out);
     return 2;
 }

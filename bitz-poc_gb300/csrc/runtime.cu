@@ -6,6 +6,7 @@
 
 #include <algorithm>
 #include <atomic>
+#include <chrono>
 #include <cstdio>
 #include <cstring>
 #include <map>
@@ -349,10 +350,18 @@ int bz_ctx_create(int device, uint64_t mem_budget_bytes, bz_ctx **out) {
         delete ctx;
         return BZ_ERR_CUDA;
     }
-    if (cudaMalloc(&ctx->d_small, 4096) != cudaSuccess) {
+    if (cudaMalloc(&ctx->d_small, 4096) != cudaSuccess ||
+        cudaMemset(ctx->d_small, 0, 4096) != cudaSuccess ||
+        cudaHostAlloc(&ctx->h_mbox, 4096, cudaHostAllocMapped) != cudaSuccess ||
+        cudaHostGetDevicePointer(&ctx->d_mbox, ctx->h_mbox, 0) != cudaSuccess) {
+        cudaGetLastError();
+        if (ctx->d_small) cudaFree(ctx->d_small);
+        if (ctx->h_mbox) cudaFreeHost(ctx->h_mbox);
+        cudaFreeHost(ctx->h_small);
         delete ctx;
         return BZ_ERR_CUDA;
     }
+    memset(ctx->h_mbox, 0, 4096);
     *out = ctx;
     return BZ_OK;
 }
@@ -377,6 +386,7 @@ int bz_ctx_destroy(bz_ctx *ctx) {
     cudaStreamSynchronize(ctx->stream);
     cudaFree(ctx->d_small);
     cudaFreeHost(ctx->h_small);
+    cudaFreeHost(ctx->h_mbox);
     cudaEventDestroy(ctx->ev0);
     cudaEventDestroy(ctx->ev1);
     cudaStreamSynchronize(ctx->copy_stream);
@@ -770,11 +780,39 @@ static uint4 to_u4(const uint64_t r[2]) {
                       (uint32_t)(r[1] >> 32));
 }
 
-static int read_msg(bz_ctx *ctx, uint64_t u0[2], uint64_t u2[2]) {
-    BZ_CUDA(ctx, cudaMemcpyAsync(ctx->h_small, ctx->d_small, 32, cudaMemcpyDeviceToHost,
-                                 ctx->stream));
-    BZ_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
-    const uint64_t *h = (const uint64_t *)ctx->h_small;
+static bool pow2(size_t n) { return n && !(n & (n - 1)); }
+
+// Mailbox post for the next message kernel on the context stream.
+static MsgPost next_post(bz_ctx *ctx) {
+    MsgPost p;
+    p.ticket = (unsigned int *)((uint8_t *)ctx->d_small + 768);
+    p.words = (uint64_t *)ctx->d_mbox;
+    p.seq = (uint32_t *)((uint8_t *)ctx->d_mbox + 64);
+    if (++ctx->mbox_seq == 0) ++ctx->mbox_seq;  // 0 is the initial mailbox value
+    p.seq_val = ctx->mbox_seq;
+    return p;
+}
+
+// Wait for the message kernel to post sequence number seq, then read
+// {u0, u2}.  The wait spins on the mailbox (no stream synchronisation on the
+// critical path), checking the stream every few hundred spins so that a
+// failed launch returns its error, and gives up after 60 s.
+static int wait_msg(bz_ctx *ctx, uint32_t seq, uint64_t u0[2], uint64_t u2[2]) {
+    volatile uint32_t *sp = (volatile uint32_t *)((uint8_t *)ctx->h_mbox + 64);
+    const auto t0 = std::chrono::steady_clock::now();
+    for (uint64_t spin = 1; *sp != seq; ++spin) {
+        if ((spin & 255) == 0) {
+            const cudaError_t e = cudaStreamQuery(ctx->stream);
+            if (e != cudaSuccess && e != cudaErrorNotReady)
+                return set_err(ctx, BZ_ERR_CUDA, "sumcheck message kernel", e);
+            if (e == cudaSuccess && *sp != seq)
+                return set_msg(ctx, BZ_ERR_CUDA, "sumcheck message not posted");
+            if (std::chrono::steady_clock::now() - t0 > std::chrono::seconds(60))
+                return set_msg(ctx, BZ_ERR_TIMEOUT, "sumcheck message wait");
+        }
+    }
+    std::atomic_thread_fence(std::memory_order_acquire);
+    const volatile uint64_t *h = (const volatile uint64_t *)ctx->h_mbox;
     if (u0) {
         u0[0] = h[0];
         u0[1] = h[1];
@@ -786,8 +824,6 @@ static int read_msg(bz_ctx *ctx, uint64_t u0[2], uint64_t u2[2]) {
     return BZ_OK;
 }
 
-static bool pow2(size_t n) { return n && !(n & (n - 1)); }
-
 int bz_fold_and_msg_lsb(bz_ctx *ctx, const uint64_t *d_f, const uint64_t *d_b, size_t n,
                         const uint64_t r[2], uint64_t *d_nf, uint64_t *d_nb, uint64_t u0[2],
                         uint64_t u2[2]) {
@@ -795,11 +831,12 @@ int bz_fold_and_msg_lsb(bz_ctx *ctx, const uint64_t *d_f, const uint64_t *d_b, s
     if (!pow2(n) || n < 2) return set_msg(ctx, BZ_ERR_SHAPE, "n must be a power of two >= 2");
     int rc = ensure_scratch(ctx, fold_partials_bytes(n));
     if (rc) return rc;
+    const MsgPost post = next_post(ctx);
     ctx->launches += launch_fold_and_msg((const uint4 *)d_f, (const uint4 *)d_b, n, to_u4(r),
                                          (uint4 *)d_nf, (uint4 *)d_nb, (uint64_t *)ctx->scratch,
-                                         (uint64_t *)ctx->d_small, ctx->stream, ctx->num_sms);
+                                         nullptr, ctx->stream, ctx->num_sms, &post);
     BZ_CUDA(ctx, cudaGetLastError());
-    return read_msg(ctx, u0, u2);
+    return wait_msg(ctx, post.seq_val, u0, u2);
 }
 
 int bz_round_msg_lsb(bz_ctx *ctx, const uint64_t *d_f, const uint64_t *d_b, size_t n,
@@ -808,11 +845,12 @@ int bz_round_msg_lsb(bz_ctx *ctx, const uint64_t *d_f, const uint64_t *d_b, size
     if (!pow2(n) || n < 2) return set_msg(ctx, BZ_ERR_SHAPE, "n must be a power of two >= 2");
     int rc = ensure_scratch(ctx, fold_partials_bytes(n));
     if (rc) return rc;
+    const MsgPost post = next_post(ctx);
     ctx->launches += launch_round_msg((const uint4 *)d_f, (const uint4 *)d_b, n,
-                                      (uint64_t *)ctx->scratch, (uint64_t *)ctx->d_small,
-                                      ctx->stream, ctx->num_sms);
+                                      (uint64_t *)ctx->scratch, nullptr, ctx->stream, ctx->num_sms,
+                                      &post);
     BZ_CUDA(ctx, cudaGetLastError());
-    return read_msg(ctx, u0, u2);
+    return wait_msg(ctx, post.seq_val, u0, u2);
 }
 
 int bz_partial_eval_lsb(bz_ctx *ctx, const uint64_t *d_in, size_t n, const uint64_t *rs, size_t k,

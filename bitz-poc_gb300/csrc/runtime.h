@@ -46,7 +46,10 @@ struct bz_ctx {
     uint8_t *scratch = nullptr;
     size_t scratch_bytes = 0;
     void *h_small = nullptr;  // 4 KiB pinned
-    void *d_small = nullptr;  // 4 KiB device
+    void *d_small = nullptr;  // 4 KiB device (zeroed; word 192 is the message ticket)
+    void *h_mbox = nullptr;   // 4 KiB mapped pinned: sumcheck message mailbox
+    void *d_mbox = nullptr;   // its device view
+    uint32_t mbox_seq = 0;    // last posted sequence number
     cudaEvent_t ev0 = nullptr, ev1 = nullptr;
     std::mutex aux_mu;
     std::map<cudaStream_t, bz_aux_stream> aux;
