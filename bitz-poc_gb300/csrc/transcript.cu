@@ -33,42 +33,70 @@ constexpr uint32_t CHUNK_START = 1, CHUNK_END = 2, PARENT = 4, ROOT = 8;
 
 inline uint32_t rotr(uint32_t x, int n) { return (x >> n) | (x << (32 - n)); }
 
-inline void mix(uint32_t s[16], int a, int b, int c, int d, uint32_t x, uint32_t y) {
-    s[a] = s[a] + s[b] + x;
-    s[d] = rotr(s[d] ^ s[a], 16);
-    s[c] = s[c] + s[d];
-    s[b] = rotr(s[b] ^ s[c], 12);
-    s[a] = s[a] + s[b] + y;
-    s[d] = rotr(s[d] ^ s[a], 8);
-    s[c] = s[c] + s[d];
-    s[b] = rotr(s[b] ^ s[c], 7);
-}
+// Message word order of every round: kSigma[0] is the identity and
+// kSigma[r + 1][i] = kSigma[r][kPerm[i]].
+struct Sigma {
+    uint8_t o[7][16];
+    constexpr Sigma() : o() {
+        for (int i = 0; i < 16; ++i) o[0][i] = (uint8_t)i;
+        for (int r = 1; r < 7; ++r)
+            for (int i = 0; i < 16; ++i) o[r][i] = o[r - 1][kPerm[i]];
+    }
+};
+constexpr Sigma kSigma;
+
+#define BZH_G(a, b, c, d, x, y)      \
+    do {                             \
+        a = a + b + (x);             \
+        d = rotr(d ^ a, 16);         \
+        c = c + d;                   \
+        b = rotr(b ^ c, 12);         \
+        a = a + b + (y);             \
+        d = rotr(d ^ a, 8);          \
+        c = c + d;                   \
+        b = rotr(b ^ c, 7);          \
+    } while (0)
 
 // Full 16-word compression output: out[i] = s[i] ^ s[i+8] and
-// out[i+8] = s[i+8] ^ cv[i].
+// out[i+8] = s[i+8] ^ cv[i].  The state lives in locals and every round
+// reads the message through its fixed word order, so the compiler keeps the
+// whole state in registers.
 void compress(const uint32_t cv[8], const uint32_t block[16], uint64_t counter,
               uint32_t block_len, uint32_t flags, uint32_t out[16]) {
-    uint32_t s[16] = {cv[0], cv[1], cv[2], cv[3], cv[4], cv[5], cv[6], cv[7],
-                      kIV[0], kIV[1], kIV[2], kIV[3], (uint32_t)counter,
-                      (uint32_t)(counter >> 32), block_len, flags};
-    uint32_t m[16], t[16];
-    memcpy(m, block, sizeof m);
+    uint32_t s0 = cv[0], s1 = cv[1], s2 = cv[2], s3 = cv[3], s4 = cv[4], s5 = cv[5],
+             s6 = cv[6], s7 = cv[7];
+    uint32_t s8 = kIV[0], s9 = kIV[1], s10 = kIV[2], s11 = kIV[3];
+    uint32_t s12 = (uint32_t)counter, s13 = (uint32_t)(counter >> 32), s14 = block_len,
+             s15 = flags;
+    const uint32_t *m = block;
+#pragma GCC unroll 7
     for (int r = 0; r < 7; ++r) {
-        mix(s, 0, 4, 8, 12, m[0], m[1]);
-        mix(s, 1, 5, 9, 13, m[2], m[3]);
-        mix(s, 2, 6, 10, 14, m[4], m[5]);
-        mix(s, 3, 7, 11, 15, m[6], m[7]);
-        mix(s, 0, 5, 10, 15, m[8], m[9]);
-        mix(s, 1, 6, 11, 12, m[10], m[11]);
-        mix(s, 2, 7, 8, 13, m[12], m[13]);
-        mix(s, 3, 4, 9, 14, m[14], m[15]);
-        for (int i = 0; i < 16; ++i) t[i] = m[kPerm[i]];
-        memcpy(m, t, sizeof m);
+        const uint8_t *o = kSigma.o[r];
+        BZH_G(s0, s4, s8, s12, m[o[0]], m[o[1]]);
+        BZH_G(s1, s5, s9, s13, m[o[2]], m[o[3]]);
+        BZH_G(s2, s6, s10, s14, m[o[4]], m[o[5]]);
+        BZH_G(s3, s7, s11, s15, m[o[6]], m[o[7]]);
+        BZH_G(s0, s5, s10, s15, m[o[8]], m[o[9]]);
+        BZH_G(s1, s6, s11, s12, m[o[10]], m[o[11]]);
+        BZH_G(s2, s7, s8, s13, m[o[12]], m[o[13]]);
+        BZH_G(s3, s4, s9, s14, m[o[14]], m[o[15]]);
     }
-    for (int i = 0; i < 8; ++i) {
-        out[i] = s[i] ^ s[i + 8];
-        out[i + 8] = s[i + 8] ^ cv[i];
-    }
+    out[0] = s0 ^ s8;
+    out[1] = s1 ^ s9;
+    out[2] = s2 ^ s10;
+    out[3] = s3 ^ s11;
+    out[4] = s4 ^ s12;
+    out[5] = s5 ^ s13;
+    out[6] = s6 ^ s14;
+    out[7] = s7 ^ s15;
+    out[8] = s8 ^ cv[0];
+    out[9] = s9 ^ cv[1];
+    out[10] = s10 ^ cv[2];
+    out[11] = s11 ^ cv[3];
+    out[12] = s12 ^ cv[4];
+    out[13] = s13 ^ cv[5];
+    out[14] = s14 ^ cv[6];
+    out[15] = s15 ^ cv[7];
 }
 
 void load_words(const uint8_t *p, size_t len, uint32_t w[16]) {
