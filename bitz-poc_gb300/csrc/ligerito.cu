@@ -79,6 +79,36 @@ __global__ void tntt_layer_kernel(uint4 *data, int log_d, int layer, const uint4
     data[ib] = gf_add(gf_mul(t, s), b);
 }
 
+// The deepest kTileLog layers of the transposed forward NTT (pair spans 1,
+// 2, .., 2^(kTileLog-1)) stay inside aligned tiles of 2^kTileLog positions:
+// one CTA loads its tile into shared memory, runs those layers from the
+// deepest up with a barrier between layers, and stores it back.  Same
+// butterfly and twiddles as tntt_layer_kernel.
+constexpr int kTileLog = 9;
+__global__ void __launch_bounds__(kThreads) tntt_tile_kernel(uint4 *data, int log_d,
+                                                             const uint4 *tw) {
+    __shared__ uint4 tile[1 << kTileLog];
+    const uint64_t base = (uint64_t)blockIdx.x << kTileLog;
+    for (int i = threadIdx.x; i < (1 << kTileLog); i += blockDim.x) tile[i] = data[base + i];
+    __syncthreads();
+    for (int half_log = 0; half_log < kTileLog; ++half_log) {
+        const int layer = log_d - half_log - 1;
+        for (int p = threadIdx.x; p < (1 << (kTileLog - 1)); p += blockDim.x) {
+            const int within = p & ((1 << half_log) - 1);
+            const int ia = ((p >> half_log) << (half_log + 1)) + within;
+            const int ib = ia + (1 << half_log);
+            const uint64_t block = (base + (uint64_t)ia) >> (half_log + 1);
+            const uint4 t = tw[((uint64_t)1 << layer) + block];
+            const uint4 a = tile[ia], b = tile[ib];
+            const uint4 s = gf_add(a, b);
+            tile[ia] = s;
+            tile[ib] = gf_add(gf_mul(t, s), b);
+        }
+        __syncthreads();
+    }
+    for (int i = threadIdx.x; i < (1 << kTileLog); i += blockDim.x) data[base + i] = tile[i];
+}
+
 // out[0] = XOR of in[0..n) (one CTA)
 __global__ void __launch_bounds__(kThreads) xor_reduce_kernel(const uint4 *in, uint64_t n,
                                                               uint4 *out) {
@@ -166,7 +196,14 @@ int launch_induce_basis(uint4 *d_domain, int log_d, const uint64_t *d_pos, const
         scatter_kernel<<<grid_for(nq), kThreads, 0, st>>>(d_domain, d_pos, d_w, nq);
         ++launches;
     }
-    for (int layer = log_d - 1; layer >= 0; --layer) {
+    int layer = log_d - 1;
+    if (log_d >= kTileLog) {
+        tntt_tile_kernel<<<(unsigned)((uint64_t)1 << (log_d - kTileLog)), kThreads, 0, st>>>(
+            d_domain, log_d, d_tw);
+        ++launches;
+        layer = log_d - kTileLog - 1;
+    }
+    for (; layer >= 0; --layer) {
         tntt_layer_kernel<<<grid_for((uint64_t)1 << (log_d - 1)), kThreads, 0, st>>>(
             d_domain, log_d, layer, d_tw);
         ++launches;
