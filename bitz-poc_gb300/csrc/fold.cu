@@ -129,8 +129,10 @@ __device__ void msg_epilogue(const uint64_t *partials, const MsgMailbox &mb) {
 // nf[j] = f[2j] + (f[2j] + f[2j+1]) * r (same for b); thread k produces the
 // folded pair (2k, 2k+1) and its message terms.  The four multiplies by the
 // challenge r use r's byte tables; the two variable products of the message
-// use the generic carry-less multiply.
-__global__ void __launch_bounds__(256) fold_and_msg_kernel(const uint4 *f, const uint4 *b,
+// use the generic carry-less multiply.  Registers are capped at 128 so two
+// CTAs share an SM (a few spilled words cost less than half the warps: the
+// 2^24 first fold takes 0.30 ms instead of 0.35 ms).
+__global__ void __launch_bounds__(256, 2) fold_and_msg_kernel(const uint4 *f, const uint4 *b,
                                                            uint64_t half, uint4 r, uint4 *nf,
                                                            uint4 *nb, uint64_t *partials,
                                                            MsgMailbox mb) {
