@@ -26,7 +26,8 @@
 //     their twiddles are narrow (at depth i the twiddle has at most about
 //     2^i * ell bits): a byte times such a twiddle is an unreduced product of
 //     at most 64 bits, so one compact 256-entry table of one or two words
-//     replaces the sixteen 16-byte tables (ntt_table_pass2_nw).
+//     replaces the sixteen 16-byte tables (ntt_table_pass2_pf with WO or
+//     WAB below 4).
 //   * the "deep" pass runs the last D layers (D <= 4) on 2^D consecutive
 //     positions held in registers, the multiply being a shift-and-XOR over
 //     the narrow twiddle's set bits, with the twiddle warp-uniform.
@@ -256,82 +257,6 @@ __global__ void __launch_bounds__(THREADS, 1) ntt_table_pass(TablePassArgs a) {
     }
 }
 
-// Radix-4 table pass with the next task's four loads issued before the
-// current task's multiplies (register double buffering), so global-memory
-// latency overlaps the shared-memory lookups.
-template <int THREADS, int MINB>
-__global__ void __launch_bounds__(THREADS, MINB) ntt_table_pass2_pf(TablePassArgs a) {
-    extern __shared__ uint4 smem[];
-    uint4 *tbl = smem;
-    uint4 *bases = smem + 3 * kT16Entries;
-    __shared__ uint4 tw_buf[kTwWindow * 3];
-    __shared__ uint64_t win[2];
-    __shared__ int tz[3];
-    if (threadIdx.x == 0) win[0] = win[1] = 0;
-    T16Lane8 lane_ctx;
-    lane_ctx.init();
-    const int log_q = a.ell - a.layer - 2;
-    const int log_task_per_b = log_q + a.log_lanes;
-    const uint64_t lanes_mask = ((uint64_t)1 << a.log_lanes) - 1;
-    const uint64_t q_mask = ((uint64_t)1 << log_q) - 1;
-    const uint64_t src_mask = ((uint64_t)1 << a.src_pos_bits) - 1;
-    const uint64_t chunks = a.n_tasks / blockDim.x;
-    const uint64_t c_beg = chunks * blockIdx.x / gridDim.x;
-    const uint64_t c_end = chunks * (blockIdx.x + 1) / gridDim.x;
-    const uint64_t b_last = (a.task_base + c_end * blockDim.x - 1) >> log_task_per_b;
-    int64_t cur_b = -1;
-    auto src_index = [&](uint64_t task, int g) -> uint64_t {
-        const uint64_t B = task >> log_task_per_b;
-        const uint64_t rr = (task >> a.log_lanes) & q_mask;
-        const uint64_t p = (B << (log_q + 2)) + ((uint64_t)g << log_q) + rr;
-        return ((p & src_mask) << a.log_lanes) | (task & lanes_mask);
-    };
-    uint4 nxt[4];
-    if (c_beg < c_end) {
-        const uint64_t t0 = a.task_base + c_beg * blockDim.x + threadIdx.x;
-#pragma unroll
-        for (int g = 0; g < 4; ++g) nxt[g] = __ldcs(a.src + src_index(t0, g));
-    }
-    for (uint64_t c = c_beg; c < c_end; ++c) {
-        const uint64_t task = a.task_base + c * blockDim.x + threadIdx.x;
-        const uint64_t B = task >> log_task_per_b;  // uniform across the CTA
-        uint4 v[4];
-#pragma unroll
-        for (int g = 0; g < 4; ++g) v[g] = nxt[g];
-        if (c + 1 < c_end) {
-            const uint64_t tn = task + blockDim.x;
-#pragma unroll
-            for (int g = 0; g < 4; ++g) nxt[g] = __ldcs(a.src + src_index(tn, g));
-        }
-        if ((int64_t)B != cur_b) {
-            __syncthreads();
-            const uint4 *ts = tw_window<3>(a.tw, a.layer, B, b_last, tw_buf, win);
-            if (threadIdx.x < 3) tz[threadIdx.x] = gf_is_zero(ts[threadIdx.x]);
-            t16_build(tbl, bases, ts, 3);  // its barriers publish tz
-            cur_b = (int64_t)B;
-        }
-        const char *T0 = reinterpret_cast<const char *>(tbl);
-        const char *T1 = T0 + kT16Entries * 16, *T2 = T1 + kT16Entries * 16;
-        if (!tz[0]) {
-            v[0] = gf_add(v[0], lane_ctx.mul(T0, v[2]));
-            v[1] = gf_add(v[1], lane_ctx.mul(T0, v[3]));
-        }
-        v[2] = gf_add(v[2], v[0]);
-        v[3] = gf_add(v[3], v[1]);
-        if (!tz[1]) v[0] = gf_add(v[0], lane_ctx.mul(T1, v[1]));
-        v[1] = gf_add(v[1], v[0]);
-        if (!tz[2]) v[2] = gf_add(v[2], lane_ctx.mul(T2, v[3]));
-        v[3] = gf_add(v[3], v[2]);
-        const uint64_t rr = (task >> a.log_lanes) & q_mask;
-        const uint64_t ln = task & lanes_mask;
-#pragma unroll
-        for (int g = 0; g < 4; ++g) {
-            const uint64_t p = (B << (log_q + 2)) + ((uint64_t)g << log_q) + rr;
-            __stcs(a.dst + ((p << a.log_lanes) | ln), v[g]);
-        }
-    }
-}
-
 // ---- Compact tables for narrow twiddles ------------------------------------
 // The deepest layers have narrow twiddles (about ell, 2 ell - 3, 4 ell - 11
 // bits at depths 0, 1, 2).  For a twiddle t of w bits, a byte x multiplies
@@ -409,24 +334,35 @@ __device__ __forceinline__ uint4 nw_mul(const char *tb, uint4 v) {
     return make_uint4(acc[0] ^ (uint32_t)f, acc[1] ^ (uint32_t)(f >> 32), acc[2], acc[3]);
 }
 
-// Radix-4 pass whose second-layer twiddles t_a, t_b are narrow (compact
-// tables of width WAB) and whose t_o uses a compact table of width WO, or
-// its 64 KB byte table when WO == 4.  Loads of the next task in flight, as
-// in ntt_table_pass2_pf.
-template <int WO, int WAB>
-__global__ void __launch_bounds__(512, 1) ntt_table_pass2_nw(TablePassArgs a) {
-    constexpr bool FULL_O = WO == 4;
+// Radix-4 table pass with the next task's four loads issued before the
+// current task's multiplies (register double buffering), so global-memory
+// latency overlaps the shared-memory lookups.  Each of the three twiddles
+// multiplies through its 64 KB byte table (width 4) or, when it is narrow,
+// through a compact table of WO (t_o) or WAB (t_a, t_b) words; t_a and t_b
+// are one layer deeper than t_o, so WAB <= WO.  Shared memory holds the byte
+// tables first (those of t_o, then t_a and t_b when WAB == 4), then their
+// basis scratch, then the compact tables.
+template <int THREADS, int MINB, int WO, int WAB>
+__global__ void __launch_bounds__(THREADS, MINB) ntt_table_pass2_pf(TablePassArgs a) {
+    static_assert(WAB <= WO, "t_a and t_b are never wider than t_o");
+    constexpr int NFULL = (WO == 4) + 2 * (WAB == 4);   // byte tables, in order o, a, b
+    constexpr int NCOMPACT = 3 - NFULL;
     extern __shared__ uint4 smem[];
-    uint4 *tbl = smem;  // t_o byte table (FULL_O)
-    uint4 *bases = smem + (FULL_O ? kT16Entries : 0);
-    char *cw = reinterpret_cast<char *>(smem + (FULL_O ? kT16Entries + kT16Bases : 0));
-    char *cw_a = cw, *cw_b = cw + kNwBytes, *cw_o = cw + 2 * kNwBytes;
+    uint4 *tbl = smem;
+    uint4 *bases = smem + NFULL * kT16Entries;
+    char *cw = reinterpret_cast<char *>(bases + NFULL * kT16Bases);
+    // compact tables in order (o when WO < 4), a, b
+    char *cw_o = cw;
+    char *cw_a = cw + (WO == 4 ? 0 : kNwBytes);
+    char *cw_b = cw_a + kNwBytes;
+    const char *T0 = reinterpret_cast<const char *>(tbl);
+    const char *T1 = T0 + kT16Entries * 16, *T2 = T1 + kT16Entries * 16;
     __shared__ uint4 tw_buf[kTwWindow * 3];
     __shared__ uint64_t win[2];
     __shared__ int tz[3];
     if (threadIdx.x == 0) win[0] = win[1] = 0;
     T16Lane8 lane_ctx;
-    if (FULL_O) lane_ctx.init();
+    if (NFULL) lane_ctx.init();
     const int log_q = a.ell - a.layer - 2;
     const int log_task_per_b = log_q + a.log_lanes;
     const uint64_t lanes_mask = ((uint64_t)1 << a.log_lanes) - 1;
@@ -465,16 +401,17 @@ __global__ void __launch_bounds__(512, 1) ntt_table_pass2_nw(TablePassArgs a) {
             __syncthreads();
             const uint4 *ts = tw_window<3>(a.tw, a.layer, B, b_last, tw_buf, win);
             if (threadIdx.x < 3) tz[threadIdx.x] = gf_is_zero(ts[threadIdx.x]);
-            if constexpr (FULL_O) t16_build(tbl, bases, ts, 1);
-            else nw_build<WO>(cw_o, lo64(ts[0]));
-            nw_build<WAB>(cw_a, lo64(ts[1]));
-            nw_build<WAB>(cw_b, lo64(ts[2]));
-            __syncthreads();
+            if constexpr (NFULL > 0) t16_build(tbl, bases, ts, NFULL);  // syncs inside
+            if constexpr (WO < 4) nw_build<WO>(cw_o, lo64(ts[0]));
+            if constexpr (WAB < 4) {
+                nw_build<WAB>(cw_a, lo64(ts[1]));
+                nw_build<WAB>(cw_b, lo64(ts[2]));
+            }
+            if constexpr (NCOMPACT > 0) __syncthreads();
             cur_b = (int64_t)B;
         }
         if (!tz[0]) {
-            if constexpr (FULL_O) {
-                const char *T0 = reinterpret_cast<const char *>(tbl);
+            if constexpr (WO == 4) {
                 v[0] = gf_add(v[0], lane_ctx.mul(T0, v[2]));
                 v[1] = gf_add(v[1], lane_ctx.mul(T0, v[3]));
             } else {
@@ -484,9 +421,15 @@ __global__ void __launch_bounds__(512, 1) ntt_table_pass2_nw(TablePassArgs a) {
         }
         v[2] = gf_add(v[2], v[0]);
         v[3] = gf_add(v[3], v[1]);
-        if (!tz[1]) v[0] = gf_add(v[0], nw_mul<WAB>(cw_a, v[1]));
-        v[1] = gf_add(v[1], v[0]);
-        if (!tz[2]) v[2] = gf_add(v[2], nw_mul<WAB>(cw_b, v[3]));
+        if constexpr (WAB == 4) {
+            if (!tz[1]) v[0] = gf_add(v[0], lane_ctx.mul(T1, v[1]));
+            v[1] = gf_add(v[1], v[0]);
+            if (!tz[2]) v[2] = gf_add(v[2], lane_ctx.mul(T2, v[3]));
+        } else {
+            if (!tz[1]) v[0] = gf_add(v[0], nw_mul<WAB>(cw_a, v[1]));
+            v[1] = gf_add(v[1], v[0]);
+            if (!tz[2]) v[2] = gf_add(v[2], nw_mul<WAB>(cw_b, v[3]));
+        }
         v[3] = gf_add(v[3], v[2]);
         const uint64_t rr = (task >> a.log_lanes) & q_mask;
         const uint64_t ln = task & lanes_mask;
@@ -695,11 +638,11 @@ static size_t table_smem(int layers) {
     return (size_t)nt * kT16Entries * 16 + (size_t)nt * kT16Bases * 16;
 }
 
-static size_t narrow_smem(bool full_o) {
-    return full_o ? (size_t)(kT16Entries + kT16Bases) * 16 + (size_t)2 * kNwBytes
-                  : (size_t)3 * kNwBytes;
+// Dynamic shared memory of ntt_table_pass2_pf<.., WO, WAB>.
+static size_t pf_smem(int wo, int wab) {
+    const int nfull = (wo == 4) + 2 * (wab == 4);
+    return (size_t)nfull * (kT16Entries + kT16Bases) * 16 + (size_t)(3 - nfull) * kNwBytes;
 }
-
 #define BZ_TAIL_ATTR(DT, DN, M)                                                           \
     cudaFuncSetAttribute(ntt_tail_pass<DT, DN, M>, cudaFuncAttributeMaxDynamicSharedMemorySize, \
                          (int)table_smem(DT))
@@ -712,23 +655,20 @@ void init_ntt_kernels() {
                          (int)table_smem(1));
     cudaFuncSetAttribute(ntt_table_pass<2, 256>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                          (int)table_smem(2));
-    cudaFuncSetAttribute(ntt_table_pass2_pf<256, 1>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                         (int)table_smem(2));
-    cudaFuncSetAttribute(ntt_table_pass2_pf<256, 2>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                         (int)table_smem(2));
-    cudaFuncSetAttribute(ntt_table_pass2_pf<512, 1>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                         (int)table_smem(2));
     cudaFuncSetAttribute(ntt_table_pass<1, 256>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                          (int)table_smem(1));
-#define BZ_NW_ATTR(WO, WAB)                                                               \
-    cudaFuncSetAttribute(ntt_table_pass2_nw<WO, WAB>,                                       \
-                         cudaFuncAttributeMaxDynamicSharedMemorySize, (int)narrow_smem(WO == 4))
-    BZ_NW_ATTR(1, 1);
-    BZ_NW_ATTR(2, 1);
-    BZ_NW_ATTR(4, 1);
-    BZ_NW_ATTR(2, 2);
-    BZ_NW_ATTR(4, 2);
-#undef BZ_NW_ATTR
+#define BZ_PF_ATTR(T, M, WO, WAB)                                                          \
+    cudaFuncSetAttribute(ntt_table_pass2_pf<T, M, WO, WAB>,                                  \
+                         cudaFuncAttributeMaxDynamicSharedMemorySize, (int)pf_smem(WO, WAB))
+    BZ_PF_ATTR(512, 1, 4, 4);
+    BZ_PF_ATTR(256, 1, 4, 4);
+    BZ_PF_ATTR(256, 2, 4, 4);
+    BZ_PF_ATTR(512, 1, 1, 1);
+    BZ_PF_ATTR(512, 1, 2, 1);
+    BZ_PF_ATTR(512, 1, 4, 1);
+    BZ_PF_ATTR(512, 1, 2, 2);
+    BZ_PF_ATTR(512, 1, 4, 2);
+#undef BZ_PF_ATTR
     BZ_TAIL_ATTR_M(1, 1); BZ_TAIL_ATTR_M(1, 2); BZ_TAIL_ATTR_M(1, 3);
     BZ_TAIL_ATTR_M(2, 1); BZ_TAIL_ATTR_M(2, 2);
 }
@@ -748,8 +688,9 @@ static void launch_tail(const DeepArgs &a, int mode, unsigned grid, cudaStream_t
     else ntt_tail_pass<DT, DN, 0><<<grid, 512, sm, st>>>(a);
 }
 
-// Whether a table pass runs as ntt_table_pass2_nw (compact tables for the
-// narrow twiddles of its second layer, and of its first when narrow too).
+// Whether a table pass runs with compact tables (ntt_table_pass2_pf with
+// WAB < 4): those of the narrow twiddles of its second layer, and of its
+// first when narrow too.
 bool narrow_table_pass(const Shape &s, uint32_t schedule, int layer, int layers, int threads) {
     return (schedule & SCHED_NARROW) && layers == 2 && threads == 512 &&
            narrow_class(twiddle_bits(s.k_code(), layer + 1)) <= 2;
@@ -778,19 +719,20 @@ int launch_table_pass(const Shape &s, int layer, int layers, const uint4 *src, i
     if (narrow_table_pass(s, schedule, layer, layers, threads)) {
         const int wo = narrow_class(twiddle_bits(ell, layer));
         const int wab = narrow_class(twiddle_bits(ell, layer + 1));
-        const size_t sm = narrow_smem(wo == 4);
-        if (wab == 1 && wo == 1) ntt_table_pass2_nw<1, 1><<<grid, 512, sm, st>>>(a);
-        else if (wab == 1 && wo == 2) ntt_table_pass2_nw<2, 1><<<grid, 512, sm, st>>>(a);
-        else if (wab == 1) ntt_table_pass2_nw<4, 1><<<grid, 512, sm, st>>>(a);
-        else if (wo == 2) ntt_table_pass2_nw<2, 2><<<grid, 512, sm, st>>>(a);
-        else ntt_table_pass2_nw<4, 2><<<grid, 512, sm, st>>>(a);
+        const size_t sm = pf_smem(wo, wab);
+        if (wab == 1 && wo == 1) ntt_table_pass2_pf<512, 1, 1, 1><<<grid, 512, sm, st>>>(a);
+        else if (wab == 1 && wo == 2) ntt_table_pass2_pf<512, 1, 2, 1><<<grid, 512, sm, st>>>(a);
+        else if (wab == 1) ntt_table_pass2_pf<512, 1, 4, 1><<<grid, 512, sm, st>>>(a);
+        else if (wo == 2) ntt_table_pass2_pf<512, 1, 2, 2><<<grid, 512, sm, st>>>(a);
+        else ntt_table_pass2_pf<512, 1, 4, 2><<<grid, 512, sm, st>>>(a);
     } else if (prefetch && layers == 2) {
+        const size_t sm = pf_smem(4, 4);
         if (threads == 256 && lean)
-            ntt_table_pass2_pf<256, 2><<<grid, 256, table_smem(2), st>>>(a);
+            ntt_table_pass2_pf<256, 2, 4, 4><<<grid, 256, sm, st>>>(a);
         else if (threads == 256)
-            ntt_table_pass2_pf<256, 1><<<grid, 256, table_smem(2), st>>>(a);
+            ntt_table_pass2_pf<256, 1, 4, 4><<<grid, 256, sm, st>>>(a);
         else
-            ntt_table_pass2_pf<512, 1><<<grid, 512, table_smem(2), st>>>(a);
+            ntt_table_pass2_pf<512, 1, 4, 4><<<grid, 512, sm, st>>>(a);
     } else if (threads == 256) {
         if (layers == 2) ntt_table_pass<2, 256><<<grid, 256, table_smem(2), st>>>(a);
         else ntt_table_pass<1, 256><<<grid, 256, table_smem(1), st>>>(a);
