@@ -130,15 +130,39 @@ def _view(p: LigeritoProof):
     return v, keep
 
 
-def _rows_from(rv: RowsView) -> list:
+class _ProofOwner:
+    """Owns a native LigeritoProof whose opened rows decoded arrays view in
+    place: the proof is freed when the last such array is gone."""
+
+    def __init__(self, h):
+        self.h = h
+
+    def __del__(self):
+        if self.h:
+            try:
+                lib().bz_ligerito_proof_free(self.h)
+            except Exception:  # interpreter shutdown: the process frees it
+                pass
+            self.h = None
+
+
+def _rows_from(rv: RowsView, owner: _ProofOwner | None = None) -> list:
+    """Opened rows as (lanes, 2) arrays: views into the native proof when an
+    owner keeps it alive (no copy of the rows), copies otherwise."""
     if not rv.n_rows:
         return []
     lens = np.ctypeslib.as_array(rv.row_lens, shape=(rv.n_rows,)).astype(np.int64)
     total = int(lens.sum())
     if not total:
         return [np.zeros((0, 2), np.uint64) for _ in range(rv.n_rows)]
-    flat = np.ctypeslib.as_array(rv.data, shape=(2 * total,)).reshape(total, 2).copy()
-    return np.split(flat, np.cumsum(lens)[:-1])
+    if owner is None:
+        flat = np.ctypeslib.as_array(rv.data, shape=(2 * total,)).copy()
+    else:
+        buf = (ctypes.c_uint64 * (2 * total)).from_address(
+            ctypes.cast(rv.data, ctypes.c_void_p).value)
+        buf._owner = owner
+        flat = np.frombuffer(buf, dtype=np.uint64)
+    return np.split(flat.reshape(total, 2), np.cumsum(lens)[:-1])
 
 
 def _hashes_from(n, ptr) -> np.ndarray:
@@ -154,10 +178,10 @@ def _words_from(n, ptr, per) -> np.ndarray:
     return a if per == 1 else a.reshape(n, per)
 
 
-def _from_view(v: ProofView) -> LigeritoProof:
+def _from_view(v: ProofView, owner: _ProofOwner | None = None) -> LigeritoProof:
     p = LigeritoProof()
     p.initial_root = bytes(v.initial_root)
-    p.initial_proof = RecursiveProof(_rows_from(v.initial_proof.rows),
+    p.initial_proof = RecursiveProof(_rows_from(v.initial_proof.rows, owner),
                                      _hashes_from(v.initial_proof.n_hashes, v.initial_proof.hashes))
     p.recursive_roots = _hashes_from(v.n_recursive_roots, v.recursive_roots)
     p.recursive_proofs = [RecursiveProof(_rows_from(v.recursive_proofs[i].rows),
@@ -185,12 +209,13 @@ def encode_ligerito(p: LigeritoProof) -> bytes:
 
 
 def _decoded(h) -> LigeritoProof:
-    try:
-        v = ProofView()
-        check(None, lib().bz_ligerito_proof_view_of(h, ctypes.byref(v)))
-        return _from_view(v)
-    finally:
-        lib().bz_ligerito_proof_free(h)
+    """Decode a native proof handle; the level-0 opened rows (the bulk of
+    the proof) stay in the native proof, which the returned arrays keep
+    alive."""
+    owner = _ProofOwner(h)
+    v = ProofView()
+    check(None, lib().bz_ligerito_proof_view_of(h, ctypes.byref(v)))
+    return _from_view(v, owner)
 
 
 def decode_ligerito(blob: bytes) -> LigeritoProof:

@@ -30,7 +30,11 @@ void put_u64(std::vector<uint8_t> &o, uint64_t v) {
 }
 
 void put_words(std::vector<uint8_t> &o, const uint64_t *w, size_t n) {
-    for (size_t i = 0; i < n; ++i) put_u64(o, w[i]);
+    const size_t base = o.size();
+    o.resize(base + 8 * n);
+    uint8_t *d = o.data() + base;
+    for (size_t i = 0; i < n; ++i)
+        for (int b = 0; b < 8; ++b) d[8 * i + b] = (uint8_t)(w[i] >> (8 * b));
 }
 
 void put_rows(std::vector<uint8_t> &o, const bz_rows_view &r) {
@@ -77,14 +81,20 @@ struct Cursor {
         if (!u64(c)) return false;
         return item == 0 || c <= (n - cur) / item;
     }
+    // n_words little-endian words appended to out (one geometric resize per
+    // call: appending row after row stays linear in the blob size)
     template <class Vec>
     bool words(Vec &out, uint64_t n_words) {
-        out.reserve(out.size() + n_words);
+        if ((n - cur) / 8 < n_words) return false;
+        const size_t base = out.size();
+        out.resize(base + n_words);
+        const uint8_t *q = p + cur;
         for (uint64_t i = 0; i < n_words; ++i) {
-            uint64_t w;
-            if (!u64(w)) return false;
-            out.push_back(w);
+            uint64_t w = 0;
+            for (int b = 0; b < 8; ++b) w |= (uint64_t)q[8 * i + b] << (8 * b);
+            out[base + i] = w;
         }
+        cur += 8 * n_words;
         return true;
     }
 };
@@ -202,6 +212,29 @@ extern "C" {
 int bz_ligerito_proof_encode(const bz_ligerito_proof_view *view, uint8_t *out, size_t cap,
                              size_t *len) {
     if (!len) return BZ_ERR_ARG;
+    if (!out) {  // size query: the byte count follows from the view's lengths
+        if (!view || !rows_ok(view->initial_proof.rows) || !rows_ok(view->final_rows.rows) ||
+            (view->n_recursive_proofs && !view->recursive_proofs))
+            return BZ_ERR_ARG;
+        for (size_t i = 0; i < view->n_recursive_proofs; ++i)
+            if (!rows_ok(view->recursive_proofs[i].rows)) return BZ_ERR_ARG;
+        auto rows_bytes = [](const bz_rows_view &r) {
+            size_t b = 8;
+            for (size_t i = 0; i < r.n_rows; ++i) b += 8 + 16 * (size_t)r.row_lens[i];
+            return b;
+        };
+        size_t n = 32 + rows_bytes(view->initial_proof.rows) + 8 + 32 * view->initial_proof.n_hashes +
+                   8 + 32 * view->n_recursive_roots + 8;
+        for (size_t i = 0; i < view->n_recursive_proofs; ++i)
+            n += rows_bytes(view->recursive_proofs[i].rows) + 8 +
+                 32 * view->recursive_proofs[i].n_hashes;
+        n += 8 + 16 * view->n_yr + rows_bytes(view->final_rows.rows) + 8 +
+             32 * view->final_rows.n_hashes + 8 + 32 * view->n_sumcheck + 8 +
+             8 * view->n_grinding_nonces + 8 + 16 * view->n_ood_values + 8 +
+             8 * view->n_fold_grinding_nonces;
+        *len = n;
+        return BZ_OK;
+    }
     std::vector<uint8_t> o;
     int rc = encode_blob(view, o);
     if (rc) return rc;
