@@ -359,8 +359,8 @@ __global__ void __launch_bounds__(THREADS, MINB) ntt_table_pass2_pf(TablePassArg
     const char *T1 = T0 + kT16Entries * 16, *T2 = T1 + kT16Entries * 16;
     __shared__ uint4 tw_buf[kTwWindow * 3];
     __shared__ uint64_t win[2];
-    __shared__ int tz[3];
     if (threadIdx.x == 0) win[0] = win[1] = 0;
+    bool z0 = false, z1 = false, z2 = false;  // zero twiddles of the current block
     T16Lane8 lane_ctx;
     if (NFULL) lane_ctx.init();
     const int log_q = a.ell - a.layer - 2;
@@ -400,7 +400,9 @@ __global__ void __launch_bounds__(THREADS, MINB) ntt_table_pass2_pf(TablePassArg
         if ((int64_t)B != cur_b) {
             __syncthreads();
             const uint4 *ts = tw_window<3>(a.tw, a.layer, B, b_last, tw_buf, win);
-            if (threadIdx.x < 3) tz[threadIdx.x] = gf_is_zero(ts[threadIdx.x]);
+            z0 = gf_is_zero(ts[0]);
+            z1 = gf_is_zero(ts[1]);
+            z2 = gf_is_zero(ts[2]);
             if constexpr (NFULL > 0) t16_build(tbl, bases, ts, NFULL);  // syncs inside
             if constexpr (WO < 4) nw_build<WO>(cw_o, lo64(ts[0]));
             if constexpr (WAB < 4) {
@@ -410,7 +412,7 @@ __global__ void __launch_bounds__(THREADS, MINB) ntt_table_pass2_pf(TablePassArg
             if constexpr (NCOMPACT > 0) __syncthreads();
             cur_b = (int64_t)B;
         }
-        if (!tz[0]) {
+        if (!z0) {
             if constexpr (WO == 4) {
                 v[0] = gf_add(v[0], lane_ctx.mul(T0, v[2]));
                 v[1] = gf_add(v[1], lane_ctx.mul(T0, v[3]));
@@ -422,13 +424,13 @@ __global__ void __launch_bounds__(THREADS, MINB) ntt_table_pass2_pf(TablePassArg
         v[2] = gf_add(v[2], v[0]);
         v[3] = gf_add(v[3], v[1]);
         if constexpr (WAB == 4) {
-            if (!tz[1]) v[0] = gf_add(v[0], lane_ctx.mul(T1, v[1]));
+            if (!z1) v[0] = gf_add(v[0], lane_ctx.mul(T1, v[1]));
             v[1] = gf_add(v[1], v[0]);
-            if (!tz[2]) v[2] = gf_add(v[2], lane_ctx.mul(T2, v[3]));
+            if (!z2) v[2] = gf_add(v[2], lane_ctx.mul(T2, v[3]));
         } else {
-            if (!tz[1]) v[0] = gf_add(v[0], nw_mul<WAB>(cw_a, v[1]));
+            if (!z1) v[0] = gf_add(v[0], nw_mul<WAB>(cw_a, v[1]));
             v[1] = gf_add(v[1], v[0]);
-            if (!tz[2]) v[2] = gf_add(v[2], nw_mul<WAB>(cw_b, v[3]));
+            if (!z2) v[2] = gf_add(v[2], nw_mul<WAB>(cw_b, v[3]));
         }
         v[3] = gf_add(v[3], v[2]);
         const uint64_t rr = (task >> a.log_lanes) & q_mask;
