@@ -235,3 +235,33 @@ def test_ring_switch_needs_128(C):
     with pytest.raises(C.BzError) as e:
         C.Reader(bytes(16 * 127)).ring_switch()
     assert e.value.status == 9
+
+
+def test_benchmark_size_proof_round_trip_is_linear_time(C):
+    """A proof of the 2^24 opening's size (148 rows of 4096 elements, 9.9 MB)
+    encodes, decodes and round-trips; the decoder appends row after row, so
+    its time must stay linear in the blob (well under a second here)."""
+    import time
+
+    rng = np.random.default_rng(17)
+    rows = [rng.integers(0, 2**64, (4096, 2), dtype=np.uint64) for _ in range(148)]
+    p = C.LigeritoProof(
+        initial_root=bytes(range(32)),
+        initial_proof=C.RecursiveProof(rows, rng.integers(0, 256, (1500, 32), dtype=np.uint8)),
+        recursive_roots=np.zeros((1, 32), np.uint8),
+        recursive_proofs=[],
+        final_proof=C.FinalProof(rng.integers(0, 2**64, (64, 2), dtype=np.uint64),
+                                 [rng.integers(0, 2**64, (64, 2), dtype=np.uint64)
+                                  for _ in range(148)],
+                                 rng.integers(0, 256, (600, 32), dtype=np.uint8)),
+        sumcheck_transcript=rng.integers(0, 2**64, (19, 2, 2), dtype=np.uint64),
+        grinding_nonces=np.array([1, 2], np.uint64),
+        ood_values=np.zeros((0, 2), np.uint64),
+        fold_grinding_nonces=np.zeros(0, np.uint64))
+    blob = C.encode_ligerito(p)
+    assert len(blob) > 9_800_000
+    t0 = time.perf_counter()
+    q = C.decode_ligerito(blob)
+    assert time.perf_counter() - t0 < 1.0
+    assert all((a == b).all() for a, b in zip(q.initial_proof.opened_rows, rows))
+    assert C.encode_ligerito(q) == blob
