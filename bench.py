@@ -601,8 +601,8 @@ def _bench_open(ctx, bz, msg, params):
     recursive Ligerito proof of the resident commitment through
     bz_ligerito_prove (open_config), and its level-0 part alone through
     bz_ligerito_open_l0.  Host wall time of each call (they synchronize for
-    every transcript squeeze), median of 3 after one warm-up.  Also times the
-    GPU proof-of-work search alone at 24 bits."""
+    every transcript squeeze), median of OPEN_REPS after one warm-up.  Also
+    times the GPU proof-of-work search alone at 24 bits."""
     import numpy as np
 
     from bitz_gb300 import codec
@@ -611,7 +611,7 @@ def _bench_open(ctx, bz, msg, params):
     c, pd = bz.commit(msg, params, ctx)
     cfg = bz.LigeritoConfig(**open_config(params.log_batch_size))
 
-    def timed(fn, reps=4):
+    def timed(fn, reps=OPEN_REPS + 1):
         ts, out = [], None
         for _ in range(reps):
             t = bz.Blake3Transcript()
@@ -632,7 +632,7 @@ def _bench_open(ctx, bz, msg, params):
                          grinding_bits0=16, queries0=148, hash_kind=HASH)
     l0_ms, l0_min, _ = timed(lambda t: bz.open_l0(t, pd, msg, b, [1, 2], l0_cfg, ctx))
     info = {"prove_ms": prove_ms, "prove_ms_min": prove_min, "prove_c_abi_ms": prove_c_ms,
-            "proof_bytes": len(blob),
+            "reps": OPEN_REPS, "proof_bytes": len(blob),
             "open_l0_ms": l0_ms, "open_l0_ms_min": l0_min, "config": OPEN_CONFIG_TEXT}
     # proof-of-work search alone: hashes scanned >= smallest nonce + 1
     pw = []
@@ -648,6 +648,7 @@ def _bench_open(ctx, bz, msg, params):
     return info
 
 
+OPEN_REPS = 20   # timed repetitions of every opening call (after one warm-up)
 BIT_MLE_CONFIG = dict(initial_k=10, recursive_ks=[5], log_inv_rates=[2, 2], queries=[148, 64],
                       grinding_bits=[16, 8], fold_grinding_bits=[0, 2], ood_samples=[0, 1],
                       hash_kind=1)
@@ -658,7 +659,8 @@ def _bench_bit_mle(ctx, bz):
     """The 2^20-word witness (2^10 lanes x 2^10 columns, rate 1/4, ChaCha seed
     0) opened at one random point through BinaryPcs: commit, round 0 (8-bit
     grind), open_bit_mle (ring switch + open_basis + recursive Ligerito,
-    BIT_MLE_CONFIG).  Host wall time per call, median of 3 after a warm-up."""
+    BIT_MLE_CONFIG).  Host wall time per call, median of OPEN_REPS after a
+    warm-up, with p99 (the slowest rep at this count)."""
     from bitz_gb300 import codec
 
     m = 20
@@ -667,7 +669,7 @@ def _bench_bit_mle(ctx, bz):
     point = np.random.default_rng(0).integers(0, 2**64, (m + 7, 2), dtype=np.uint64)
     ts = {"commit_ms": [], "round0_ms": [], "open_bit_mle_ms": []}
     nbytes = 0
-    for _ in range(4):
+    for _ in range(OPEN_REPS + 1):
         ctx.synchronize()
         t0 = time.perf_counter()
         c, pd = pcs.commit(d)
@@ -687,6 +689,8 @@ def _bench_bit_mle(ctx, bz):
             ts[k].append(v * 1e3)
     d.free()
     out = {k: statistics.median(v[1:]) for k, v in ts.items()}
+    out.update({k.replace("_ms", "_p99_ms"): max(v[1:]) for k, v in ts.items()})
+    out["reps"] = OPEN_REPS
     out["proof_stream_bytes"] = nbytes
     out["config"] = "BinaryPcs round 0 (8-bit grind) + open_bit_mle, " + str(BIT_MLE_CONFIG)
     return out
