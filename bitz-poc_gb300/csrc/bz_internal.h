@@ -86,7 +86,7 @@ int launch_deep_range(const Shape &s, int deep, int mode, const uint4 *src, int 
 // and the parent levels above all leaves.
 bool leaves_range_supported(const Shape &s);
 int launch_leaves_range(const Shape &s, const uint4 *d_cw, uint8_t *d_tree, uint64_t p0,
-                        uint64_t p1, cudaStream_t st);
+                        uint64_t p1, cudaStream_t st, int num_sms);
 int launch_merkle_levels(const Shape &s, uint8_t *d_tree, cudaStream_t st, LaunchLog *log);
 // Two-stream software pipeline of one commit: after the first table pass,
 // position chunks go through the remaining table passes on `st` while the

@@ -21,14 +21,16 @@ namespace bz {
 
 // ---------------------------------------------------------------------------
 // BLAKE3 leaves, C >= 1 chunks per leaf, C <= 256.
-// Each thread computes one chunk CV; the CTA (256 threads = 256 chunks =
-// 256 / C leaves) reduces groups of C CVs to leaf CVs in shared memory.
+// Each thread computes one chunk CV; the CTA (T <= 256 threads = T chunks =
+// T / C leaves, T a power of two >= C) reduces groups of C CVs to leaf CVs in
+// shared memory.  Small trees launch smaller CTAs so the chunks spread over
+// the SMs (a chunk's 16 compressions are sequential).
 // ---------------------------------------------------------------------------
 __global__ void __launch_bounds__(256) b3_leaves_chunked(const uint4 *cw, int log_lanes,
                                                          uint64_t n_chunks, uint32_t *tree_leaves,
                                                          int log_c) {
     __shared__ uint32_t cvs[256][9];  // padded rows
-    const uint64_t chunk = (uint64_t)blockIdx.x * 256 + threadIdx.x;
+    const uint64_t chunk = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
     const uint32_t c_in_leaf = (uint32_t)(chunk & ((1u << log_c) - 1));
     uint32_t cv[8];
 #pragma unroll
@@ -57,7 +59,7 @@ __global__ void __launch_bounds__(256) b3_leaves_chunked(const uint4 *cw, int lo
     for (int s = 0; s < log_c; ++s) {
         const int stride = 1 << s;
         const int t = threadIdx.x;
-        if ((t & ((stride << 1) - 1)) == 0 && t + stride < 256) {
+        if ((t & ((stride << 1) - 1)) == 0 && t + stride < (int)blockDim.x) {
             uint32_t out[8];
             b3_parent(cvs[t], cvs[t + stride], out);
 #pragma unroll
@@ -283,10 +285,19 @@ size_t merkle_scratch_bytes(const Shape &s) {
 static int launch_levels(uint32_t *tree, uint64_t n_leaves, int kind, cudaStream_t st,
                          LaunchLog *log);
 
+// CTA size of b3_leaves_chunked: 256 threads, halved (down to 32 and to the
+// chunks per leaf) while that leaves fewer than two CTAs per SM.
+static unsigned leaf_threads(uint64_t n_chunks, int log_c, int num_sms) {
+    unsigned t = 256;
+    const unsigned floor = std::max(32u, 1u << log_c);
+    while (t > floor && n_chunks / t < 2 * (uint64_t)num_sms) t >>= 1;
+    return t;
+}
+
 bool leaves_range_supported(const Shape &s) { return !(s.hash_kind == 1 && s.log_lanes > 14); }
 
 int launch_leaves_range(const Shape &s, const uint4 *d_cw, uint8_t *d_tree, uint64_t p0,
-                        uint64_t p1, cudaStream_t st) {
+                        uint64_t p1, cudaStream_t st, int num_sms) {
     uint32_t *tree = reinterpret_cast<uint32_t *>(d_tree);
     const uint64_t n = p1 - p0;
     const uint4 *cw = d_cw + (p0 << s.log_lanes);
@@ -298,7 +309,8 @@ int launch_leaves_range(const Shape &s, const uint4 *d_cw, uint8_t *d_tree, uint
         } else {
             const int log_c = s.log_lanes - 6;
             const uint64_t n_chunks = n << log_c;
-            b3_leaves_chunked<<<(unsigned)((n_chunks + 255) / 256), 256, 0, st>>>(
+            const unsigned t = leaf_threads(n_chunks, log_c, num_sms);
+            b3_leaves_chunked<<<(unsigned)((n_chunks + t - 1) / t), t, 0, st>>>(
                 cw, s.log_lanes, n_chunks, leaves, log_c);
         }
     } else {
@@ -355,7 +367,6 @@ int launch_merkle(const Shape &s, const uint4 *d_cw, uint8_t *d_tree, uint8_t *d
     auto mark = [&](const char *n) {
         if (log) log->mark(n);
     };
-    (void)num_sms;
     const uint64_t n_leaves = s.n_leaves();
     uint32_t *tree = reinterpret_cast<uint32_t *>(d_tree);
     int launches = 0;
@@ -368,7 +379,8 @@ int launch_merkle(const Shape &s, const uint4 *d_cw, uint8_t *d_tree, uint8_t *d
         } else if (s.log_lanes <= 14) {
             const int log_c = s.log_lanes - 6;
             const uint64_t n_chunks = n_leaves << log_c;
-            b3_leaves_chunked<<<(unsigned)((n_chunks + 255) / 256), 256, 0, st>>>(
+            const unsigned t = leaf_threads(n_chunks, log_c, num_sms);
+            b3_leaves_chunked<<<(unsigned)((n_chunks + t - 1) / t), t, 0, st>>>(
                 d_cw, s.log_lanes, n_chunks, tree, log_c);
             mark("b3_leaves_chunked");
             ++launches;

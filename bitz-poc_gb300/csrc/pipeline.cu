@@ -63,7 +63,7 @@ int launch_commit_pipelined(const Shape &s, uint32_t schedule, const uint4 *d_ms
         if (deep > 0)
             launches += launch_deep_range(s, deep, mode, d_cw, 62, d_cw, d_tw, p0, p1, aux,
                                           num_sms);
-        launches += launch_leaves_range(s, d_cw, d_tree, p0, p1, aux);
+        launches += launch_leaves_range(s, d_cw, d_tree, p0, p1, aux, num_sms);
     }
     cudaEventRecord(ev[chunks], aux);
     cudaStreamWaitEvent(st, ev[chunks], 0);
