@@ -31,6 +31,8 @@
 // not computed.
 #include <cuda_runtime.h>
 
+#include <future>
+
 #include <string.h>
 
 #include <algorithm>
@@ -211,20 +213,46 @@ std::vector<uint64_t> sample_vec(bzh::Transcript *tr, uint32_t n) {
     return v;
 }
 
-// opened rows (each 2^log_lanes elements) and the multi-proof
-int open_rows(bz_commitment *c, const std::vector<uint64_t> &queries, bzp::Level &out) {
+// opened rows (each 2^log_lanes elements) and the multi-proof, on stream st
+int open_rows_on(bz_commitment *c, const std::vector<uint64_t> &queries, bzp::Level &out,
+                 cudaStream_t st) {
     const size_t q = queries.size();
     const size_t lanes = c->shape.leaf_bytes() / 16;
     out.rows.lens.assign(q, lanes);
     out.rows.data.resize(q * lanes * 2);
-    int rc = bz_commitment_rows(c, queries.data(), q, out.rows.data.data());
+    int rc = bz::commitment_rows_on(c, queries.data(), q, out.rows.data.data(), st);
     if (rc) return rc;
     size_t n_hashes = 0;
-    rc = bz_commitment_multiproof(c, queries.data(), q, nullptr, 0, &n_hashes);
+    rc = bz::commitment_multiproof_on(c, queries.data(), q, nullptr, 0, &n_hashes, st);
     if (rc) return rc;
     out.hashes.resize(n_hashes * 32);
-    return bz_commitment_multiproof(c, queries.data(), q, out.hashes.data(), n_hashes,
-                                    &n_hashes);
+    return bz::commitment_multiproof_on(c, queries.data(), q, out.hashes.data(), n_hashes,
+                                        &n_hashes, st);
+}
+
+int open_rows(bz_commitment *c, const std::vector<uint64_t> &queries, bzp::Level &out) {
+    return open_rows_on(c, queries, out, c->ctx->stream);
+}
+
+// The same opening on the context's side stream from its helper thread, so its
+// gather and its device-to-host copy of the rows (the bulk of a level-0
+// opening) overlap the work that follows on the context stream.  The side
+// stream first waits for the context stream's work enqueued so far.
+std::future<int> open_rows_async(bz_commitment *c, std::vector<uint64_t> queries,
+                                 bzp::Level &out) {
+    bz_ctx *ctx = c->ctx;
+    cudaEvent_t ready = nullptr;
+    if (cudaEventCreateWithFlags(&ready, cudaEventDisableTiming) == cudaSuccess) {
+        cudaEventRecord(ready, ctx->stream);
+        cudaStreamWaitEvent(ctx->side_stream, ready, 0);
+        cudaEventDestroy(ready);
+    } else {
+        cudaGetLastError();
+        cudaStreamSynchronize(ctx->stream);
+    }
+    return bz::side_async(ctx, [c, q = std::move(queries), &out]() {
+        return open_rows_on(c, q, out, c->ctx->side_stream);
+    });
 }
 
 // The basis a level's queries induce over its 2^log_msg_cols message columns,
@@ -277,14 +305,21 @@ struct bz_l0_opening {
     std::vector<uint64_t> queries;
     std::vector<uint64_t> alpha;       // ceil_log2(q) x {lo, hi}
     bzp::Level initial;                // opened rows + multi-proof
+    std::future<int> initial_done;     // the opening of `initial`, when still in flight
     bz_commitment *level1 = nullptr;
     uint32_t lanes = 0, log_msg_cols0 = 0, rate0 = 0;
 };
 
 namespace {
 
+// Status of the level-0 row opening (waits for it when still in flight).
+int initial_rows(bz_l0_opening *o) {
+    return o->initial_done.valid() ? o->initial_done.get() : BZ_OK;
+}
+
 void free_opening(bz_l0_opening *o) {
     if (!o) return;
+    initial_rows(o);  // the helper thread writes o->initial
     if (o->level1) bz_commitment_free(o->level1);
     o->sc.release();
     delete o;
@@ -352,7 +387,7 @@ int open_level0(bz_ctx *ctx, bz_transcript *transcript, bz_commitment *c0,
     if (rc) return fail(rc);
     o->queries = sample_queries(tr, block_len0, cfg->queries0);
     o->alpha = sample_vec(tr, ceil_log2(cfg->queries0));
-    if ((rc = open_rows(c0, o->queries, o->initial))) return fail(rc);
+    o->initial_done = open_rows_async(c0, o->queries, o->initial);
     *out = o;
     return BZ_OK;
 }
@@ -365,7 +400,13 @@ int bz_ligerito_open_l0(bz_ctx *ctx, bz_transcript *transcript, bz_commitment *c
                         const uint64_t *d_packed, const uint64_t *d_basis,
                         const uint64_t target[2], const bz_l0_config *cfg,
                         bz_l0_opening **out) {
-    return open_level0(ctx, transcript, c0, d_packed, d_basis, target, cfg, out);
+    int rc = open_level0(ctx, transcript, c0, d_packed, d_basis, target, cfg, out);
+    if (rc) return rc;
+    if ((rc = initial_rows(*out))) {
+        free_opening(*out);
+        *out = nullptr;
+    }
+    return rc;
 }
 
 int bz_l0_opening_sizes(const bz_l0_opening *o, bz_l0_sizes *sz) {
@@ -482,7 +523,6 @@ int bz_ligerito_prove(bz_ctx *ctx, bz_transcript *transcript, bz_commitment *c0,
     };
     if (!p) return finish(BZ_ERR_NOMEM);
     memcpy(p->initial_root, c0->root, 32);
-    p->initial = std::move(o->initial);
     p->recursive_roots.insert(p->recursive_roots.end(), o->root1, o->root1 + 32);
     p->grinding_nonces.push_back(o->grinding_nonce);
     p->ood_values = o->ood_values;
@@ -521,6 +561,8 @@ int bz_ligerito_prove(bz_ctx *ctx, bz_transcript *transcript, bz_commitment *c0,
             const std::vector<uint64_t> qs = sample_queries(tr, block_len, cfg->queries[i + 1]);
             if ((rc = open_rows(prev, qs, p->fin))) return finish(rc);
             p->sumcheck = sc.msgs;
+            if ((rc = initial_rows(o))) return finish(rc);
+            p->initial = std::move(o->initial);
             *out = p;
             return finish(BZ_OK);
         }

@@ -266,6 +266,122 @@ int launch_commit_kernels(bz_ctx *ctx, const Shape &s, uint32_t schedule, const 
     return n;
 }
 
+int commitment_rows_on(bz_commitment *c, const uint64_t *positions, size_t q, uint64_t *out,
+                       cudaStream_t st) {
+    bz_ctx *ctx = c->ctx;
+    const uint64_t n_pos = c->shape.n_leaves();
+    for (size_t i = 0; i < q; ++i)
+        if (positions[i] >= n_pos) return set_msg(ctx, BZ_ERR_ARG, "position out of range");
+    if (q == 0) return BZ_OK;
+    const size_t row_bytes = c->shape.leaf_bytes();
+    void *d_pos = nullptr, *d_out = nullptr;
+    if (cudaMallocAsync(&d_pos, q * 8, st) != cudaSuccess ||
+        cudaMallocAsync(&d_out, q * row_bytes, st) != cudaSuccess) {
+        cudaGetLastError();
+        if (d_pos) cudaFreeAsync(d_pos, st);
+        return set_msg(ctx, BZ_ERR_NOMEM, "opened rows buffer");
+    }
+    cudaMemcpyAsync(d_pos, positions, q * 8, cudaMemcpyHostToDevice, st);
+    ctx->launches += launch_gather_rows(c->d_cw, c->shape.log_lanes, (const uint64_t *)d_pos, q,
+                                        (uint4 *)d_out, st);
+    cudaMemcpyAsync(out, d_out, q * row_bytes, cudaMemcpyDeviceToHost, st);
+    cudaFreeAsync(d_pos, st);
+    cudaFreeAsync(d_out, st);
+    BZ_CUDA(ctx, cudaStreamSynchronize(st));
+    return BZ_OK;
+}
+
+int commitment_multiproof_on(bz_commitment *c, const uint64_t *positions, size_t q, uint8_t *out,
+                             size_t cap, size_t *n_hashes, cudaStream_t st) {
+    bz_ctx *ctx = c->ctx;
+    const uint64_t num_leaves = c->shape.n_leaves();
+    *n_hashes = 0;
+    if (q == 0 || num_leaves == 1) return BZ_OK;
+    // merkle_multi_proof (merkle.rs:688-741): sorted unique positions, walk
+    // levels bottom-up, emit the sibling of every node whose sibling is not
+    // itself active.
+    std::vector<uint64_t> act(positions, positions + q);
+    for (uint64_t p : act)
+        if (p >= num_leaves) return set_msg(ctx, BZ_ERR_ARG, "position out of range");
+    std::sort(act.begin(), act.end());
+    act.erase(std::unique(act.begin(), act.end()), act.end());
+    std::vector<uint64_t> idx;
+    uint64_t level_start = 0, level_len = num_leaves;
+    while (level_len > 1) {
+        std::vector<uint64_t> next;
+        next.reserve(act.size());
+        size_t i = 0;
+        while (i < act.size()) {
+            const uint64_t p = act[i];
+            const bool sib = i + 1 < act.size() && act[i + 1] == (p ^ 1);
+            if (sib) {
+                i += 2;
+            } else {
+                idx.push_back(level_start + (p ^ 1));
+                i += 1;
+            }
+            next.push_back(p >> 1);
+        }
+        act.swap(next);
+        level_start += level_len;
+        level_len >>= 1;
+    }
+    *n_hashes = idx.size();
+    if (!out) return BZ_OK;  // size query
+    if (idx.size() > cap) return set_msg(ctx, BZ_ERR_ARG, "multiproof buffer too small");
+    if (idx.empty()) return BZ_OK;
+    void *d_idx = nullptr, *d_out = nullptr;
+    if (cudaMallocAsync(&d_idx, idx.size() * 8, st) != cudaSuccess ||
+        cudaMallocAsync(&d_out, idx.size() * 32, st) != cudaSuccess) {
+        cudaGetLastError();
+        if (d_idx) cudaFreeAsync(d_idx, st);
+        return set_msg(ctx, BZ_ERR_NOMEM, "multiproof buffer");
+    }
+    cudaMemcpyAsync(d_idx, idx.data(), idx.size() * 8, cudaMemcpyHostToDevice, st);
+    ctx->launches += launch_gather_nodes(c->d_tree, (const uint64_t *)d_idx, idx.size(),
+                                         (uint8_t *)d_out, st);
+    cudaMemcpyAsync(out, d_out, idx.size() * 32, cudaMemcpyDeviceToHost, st);
+    cudaFreeAsync(d_idx, st);
+    cudaFreeAsync(d_out, st);
+    BZ_CUDA(ctx, cudaStreamSynchronize(st));
+    return BZ_OK;
+}
+
+std::future<int> side_async(bz_ctx *ctx, std::function<int()> job) {
+    auto task = std::make_shared<std::packaged_task<int()>>(std::move(job));
+    std::future<int> f = task->get_future();
+    {
+        std::lock_guard<std::mutex> g(ctx->side_mu);
+        if (!ctx->side_thread.joinable()) {
+            ctx->side_thread = std::thread([ctx] {
+                cudaSetDevice(ctx->device);
+                std::unique_lock<std::mutex> lk(ctx->side_mu);
+                while (true) {
+                    ctx->side_cv.wait(lk, [ctx] { return ctx->side_stop || !ctx->side_jobs.empty(); });
+                    if (ctx->side_jobs.empty()) return;  // stopping, nothing left
+                    std::function<void()> j = std::move(ctx->side_jobs.front());
+                    ctx->side_jobs.pop_front();
+                    lk.unlock();
+                    j();
+                    lk.lock();
+                }
+            });
+        }
+        ctx->side_jobs.emplace_back([task] { (*task)(); });
+    }
+    ctx->side_cv.notify_one();
+    return f;
+}
+
+void side_shutdown(bz_ctx *ctx) {
+    {
+        std::lock_guard<std::mutex> g(ctx->side_mu);
+        ctx->side_stop = true;
+    }
+    ctx->side_cv.notify_all();
+    if (ctx->side_thread.joinable()) ctx->side_thread.join();
+}
+
 int fetch_root(bz_commitment *c) {
     bz_ctx *ctx = c->ctx;
     if (c->root_ready) return BZ_OK;
@@ -330,7 +446,8 @@ int bz_ctx_create(int device, uint64_t mem_budget_bytes, bz_ctx **out) {
     cudaGetDeviceProperties(&prop, device);
     ctx->num_sms = prop.multiProcessorCount;
     if (cudaStreamCreateWithFlags(&ctx->stream, cudaStreamNonBlocking) != cudaSuccess ||
-        cudaStreamCreateWithFlags(&ctx->copy_stream, cudaStreamNonBlocking) != cudaSuccess) {
+        cudaStreamCreateWithFlags(&ctx->copy_stream, cudaStreamNonBlocking) != cudaSuccess ||
+        cudaStreamCreateWithFlags(&ctx->side_stream, cudaStreamNonBlocking) != cudaSuccess) {
         delete ctx;
         return BZ_ERR_CUDA;
     }
@@ -369,6 +486,7 @@ int bz_ctx_create(int device, uint64_t mem_budget_bytes, bz_ctx **out) {
 int bz_ctx_destroy(bz_ctx *ctx) {
     if (!ctx) return BZ_ERR_ARG;
     cudaSetDevice(ctx->device);
+    side_shutdown(ctx);  // finishes queued side-stream openings first
     cudaStreamSynchronize(ctx->stream);
     std::vector<bz_commitment *> live;
     {
@@ -391,6 +509,8 @@ int bz_ctx_destroy(bz_ctx *ctx) {
     cudaEventDestroy(ctx->ev1);
     cudaStreamSynchronize(ctx->copy_stream);
     cudaStreamDestroy(ctx->copy_stream);
+    cudaStreamSynchronize(ctx->side_stream);
+    cudaStreamDestroy(ctx->side_stream);
     cudaStreamDestroy(ctx->stream);
     delete ctx;
     return BZ_OK;
@@ -612,86 +732,13 @@ int bz_commitment_copy_tree(bz_commitment *c, uint8_t *out, size_t n_nodes) {
 
 int bz_commitment_rows(bz_commitment *c, const uint64_t *positions, size_t q, uint64_t *out) {
     if (!c || (q && (!positions || !out))) return BZ_ERR_ARG;
-    bz_ctx *ctx = c->ctx;
-    const uint64_t n_pos = c->shape.n_leaves();
-    for (size_t i = 0; i < q; ++i)
-        if (positions[i] >= n_pos) return set_msg(ctx, BZ_ERR_ARG, "position out of range");
-    if (q == 0) return BZ_OK;
-    const size_t row_bytes = c->shape.leaf_bytes();
-    void *d_pos = nullptr, *d_out = nullptr;
-    int rc = dev_alloc(ctx, q * 8, &d_pos, false);
-    if (rc) return rc;
-    rc = dev_alloc(ctx, q * row_bytes, &d_out, false);
-    if (rc) {
-        dev_free(ctx, d_pos, q * 8, false);
-        return rc;
-    }
-    cudaMemcpyAsync(d_pos, positions, q * 8, cudaMemcpyHostToDevice, ctx->stream);
-    ctx->launches += launch_gather_rows(c->d_cw, c->shape.log_lanes, (const uint64_t *)d_pos, q,
-                                        (uint4 *)d_out, ctx->stream);
-    cudaMemcpyAsync(out, d_out, q * row_bytes, cudaMemcpyDeviceToHost, ctx->stream);
-    dev_free(ctx, d_pos, q * 8, false);
-    dev_free(ctx, d_out, q * row_bytes, false);
-    BZ_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
-    return BZ_OK;
+    return bz::commitment_rows_on(c, positions, q, out, c->ctx->stream);
 }
 
 int bz_commitment_multiproof(bz_commitment *c, const uint64_t *positions, size_t q, uint8_t *out,
                              size_t cap, size_t *n_hashes) {
     if (!c || !n_hashes || (q && !positions)) return BZ_ERR_ARG;
-    bz_ctx *ctx = c->ctx;
-    const uint64_t num_leaves = c->shape.n_leaves();
-    *n_hashes = 0;
-    if (q == 0 || num_leaves == 1) return BZ_OK;
-    // merkle_multi_proof (merkle.rs:688-741): sorted unique positions, walk
-    // levels bottom-up, emit the sibling of every node whose sibling is not
-    // itself active.
-    std::vector<uint64_t> act(positions, positions + q);
-    for (uint64_t p : act)
-        if (p >= num_leaves) return set_msg(ctx, BZ_ERR_ARG, "position out of range");
-    std::sort(act.begin(), act.end());
-    act.erase(std::unique(act.begin(), act.end()), act.end());
-    std::vector<uint64_t> idx;
-    uint64_t level_start = 0, level_len = num_leaves;
-    while (level_len > 1) {
-        std::vector<uint64_t> next;
-        next.reserve(act.size());
-        size_t i = 0;
-        while (i < act.size()) {
-            const uint64_t p = act[i];
-            const bool sib = i + 1 < act.size() && act[i + 1] == (p ^ 1);
-            if (sib) {
-                i += 2;
-            } else {
-                idx.push_back(level_start + (p ^ 1));
-                i += 1;
-            }
-            next.push_back(p >> 1);
-        }
-        act.swap(next);
-        level_start += level_len;
-        level_len >>= 1;
-    }
-    *n_hashes = idx.size();
-    if (!out) return BZ_OK;  // size query
-    if (idx.size() > cap) return set_msg(ctx, BZ_ERR_ARG, "multiproof buffer too small");
-    if (idx.empty()) return BZ_OK;
-    void *d_idx = nullptr, *d_out = nullptr;
-    int rc = dev_alloc(ctx, idx.size() * 8, &d_idx, false);
-    if (rc) return rc;
-    rc = dev_alloc(ctx, idx.size() * 32, &d_out, false);
-    if (rc) {
-        dev_free(ctx, d_idx, 0, false);
-        return rc;
-    }
-    cudaMemcpyAsync(d_idx, idx.data(), idx.size() * 8, cudaMemcpyHostToDevice, ctx->stream);
-    ctx->launches += launch_gather_nodes(c->d_tree, (const uint64_t *)d_idx, idx.size(),
-                                         (uint8_t *)d_out, ctx->stream);
-    cudaMemcpyAsync(out, d_out, idx.size() * 32, cudaMemcpyDeviceToHost, ctx->stream);
-    dev_free(ctx, d_idx, 0, false);
-    dev_free(ctx, d_out, 0, false);
-    BZ_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
-    return BZ_OK;
+    return bz::commitment_multiproof_on(c, positions, q, out, cap, n_hashes, c->ctx->stream);
 }
 
 int bz_commitment_free(bz_commitment *c) {

@@ -4,6 +4,11 @@
 #include <cuda_runtime.h>
 
 #include <atomic>
+#include <thread>
+#include <future>
+#include <functional>
+#include <deque>
+#include <condition_variable>
 #include <map>
 #include <mutex>
 #include <set>
@@ -54,6 +59,14 @@ struct bz_ctx {
     std::mutex aux_mu;
     std::map<cudaStream_t, bz_aux_stream> aux;
     cudaStream_t copy_stream = nullptr;  // host-to-device uploads of async commits
+    cudaStream_t side_stream = nullptr;  // openings that overlap the context stream's work
+    // One helper thread (started on first use) runs side-stream work queued by
+    // side_async; reusing it spares a thread start per proof.
+    std::mutex side_mu;
+    std::condition_variable side_cv;
+    std::deque<std::function<void()>> side_jobs;
+    std::thread side_thread;
+    bool side_stop = false;
     uint64_t root_ring = 0;              // next 32-byte slot of h_small for async roots
 };
 
@@ -75,6 +88,15 @@ int shape_from_params(const bz_params *p, Shape &s, size_t n_words, std::string 
 int dev_alloc(bz_ctx *ctx, size_t bytes, void **p, bool budgeted);
 void dev_free(bz_ctx *ctx, void *p, size_t bytes, bool budgeted);
 int ensure_scratch(bz_ctx *ctx, size_t bytes);
+// Run job on the context's helper thread; the future holds its status.
+std::future<int> side_async(bz_ctx *ctx, std::function<int()> job);
+void side_shutdown(bz_ctx *ctx);
+// Opened rows and multi-proof of a commitment on stream st (synchronised on
+// return); the C ABI calls run them on the context stream.
+int commitment_rows_on(bz_commitment *c, const uint64_t *positions, size_t q, uint64_t *out,
+                       cudaStream_t st);
+int commitment_multiproof_on(bz_commitment *c, const uint64_t *positions, size_t q, uint8_t *out,
+                             size_t cap, size_t *n_hashes, cudaStream_t st);
 int get_twiddles(bz_ctx *ctx, int ell, const uint4 **out);
 uint32_t schedule_for(bz_ctx *ctx, const Shape &s);
 int alloc_commitment(bz_ctx *ctx, const Shape &s, bz_commitment **out);
