@@ -21,15 +21,20 @@ BZ_HD uint4 gf_add(uint4 a, uint4 b) {
 }
 BZ_HD bool gf_is_zero(uint4 a) { return (a.x | a.y | a.z | a.w) == 0; }
 
-// 32x32 -> 64 carry-less product on the integer multiplier.
+// 32x32 -> 64 carry-less product on the integer multiplier.  Class k of the
+// result collects the products a_i * b_j with i + j = k (mod 4).  One product
+// of classes (i, j) puts at most 8 partial bits on a result bit.  Two products
+// whose i + j differ by 4 put at most 15 there (8 + 7, checked over every
+// position), so such a pair is summed by the multiply-add itself: one XOR
+// fewer per pair.
 BZ_HD uint64_t clmul32(uint32_t a, uint32_t b) {
     const uint32_t M = 0x11111111u;
     const uint32_t a0 = a & M, a1 = a & (M << 1), a2 = a & (M << 2), a3 = a & (M << 3);
     const uint32_t b0 = b & M, b1 = b & (M << 1), b2 = b & (M << 2), b3 = b & (M << 3);
     auto p = [](uint32_t x, uint32_t y) -> uint64_t { return (uint64_t)x * (uint64_t)y; };
-    const uint64_t z0 = p(a0, b0) ^ p(a1, b3) ^ p(a2, b2) ^ p(a3, b1);
-    const uint64_t z1 = p(a0, b1) ^ p(a1, b0) ^ p(a2, b3) ^ p(a3, b2);
-    const uint64_t z2 = p(a0, b2) ^ p(a1, b1) ^ p(a2, b0) ^ p(a3, b3);
+    const uint64_t z0 = (p(a0, b0) + p(a1, b3)) ^ p(a2, b2) ^ p(a3, b1);
+    const uint64_t z1 = (p(a0, b1) + p(a2, b3)) ^ (p(a1, b0) + p(a3, b2));
+    const uint64_t z2 = (p(a0, b2) + p(a3, b3)) ^ p(a1, b1) ^ p(a2, b0);
     const uint64_t z3 = p(a0, b3) ^ p(a1, b2) ^ p(a2, b1) ^ p(a3, b0);
     const uint64_t W = 0x1111111111111111ull;
     return (z0 & W) | (z1 & (W << 1)) | (z2 & (W << 2)) | (z3 & (W << 3));
