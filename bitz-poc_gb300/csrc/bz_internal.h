@@ -120,10 +120,23 @@ struct MsgPost {
     uint32_t *seq;         // device view of mapped host memory
     uint32_t seq_val;
 };
+// Challenge gate of a fold launched ahead of its challenge: the host writes r
+// to mapped memory, then the sequence number to `go` (or seq | kGateCancel to
+// cancel).  The kernel waits at most kGateLimitNs, then records seq in *err.
+constexpr uint32_t kGateCancel = 0x80000000u;
+constexpr uint64_t kGateLimitNs = 5000000000ull;
+struct RGate {
+    const uint32_t *go = nullptr;  // device view of mapped host memory
+    const uint64_t *r = nullptr;   // device view of mapped host memory: r.lo, r.hi
+    uint32_t seq = 0;              // 1 .. kGateCancel - 1
+    uint32_t *err = nullptr;       // device memory
+};
 size_t fold_partials_bytes(size_t n);
+int fold_grid(size_t n, int num_sms);
 int launch_fold_and_msg(const uint4 *d_f, const uint4 *d_b, size_t n, uint4 r, uint4 *d_nf,
                         uint4 *d_nb, uint64_t *d_partials, uint64_t *d_msg_out, cudaStream_t st,
-                        int num_sms, const MsgPost *post = nullptr);
+                        int num_sms, const MsgPost *post = nullptr,
+                        const RGate *gate = nullptr);
 int launch_round_msg(const uint4 *d_f, const uint4 *d_b, size_t n, uint64_t *d_partials,
                      uint64_t *d_msg_out, cudaStream_t st, int num_sms,
                      const MsgPost *post = nullptr);

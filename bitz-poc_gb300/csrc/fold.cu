@@ -66,6 +66,25 @@ __device__ __forceinline__ const char *build_r_table(uint4 *smem, uint4 r) {
 // by shuffles and across warps.  Partials are read from L2 (other CTAs wrote
 // them in this launch or the previous one).
 constexpr int kFinishThreads = 256;
+
+// out = {u0, u2}: the two unreduced sums acc[0..3], acc[4..7], reduced.
+__device__ __forceinline__ void store_msg(const uint64_t *acc, uint64_t *out) {
+    gf_wide w0, w2;
+    for (int i = 0; i < 4; ++i) {
+        w0.w[i] = acc[i];
+        w2.w[i] = acc[4 + i];
+    }
+    const uint4 u0 = gf_reduce(w0), u2 = gf_reduce(w2);
+    out[0] = lo64(u0);
+    out[1] = hi64(u0);
+    out[2] = lo64(u2);
+    out[3] = hi64(u2);
+}
+
+__device__ __forceinline__ void st_release_sys(uint32_t *p, uint32_t v) {
+    asm volatile("st.release.sys.global.u32 [%0], %1;" ::"l"(p), "r"(v) : "memory");
+}
+
 __device__ void finish_msg_body(const uint64_t *partials, int n, uint64_t *out) {
     __shared__ uint64_t red[kFinishThreads / 32][8];
     __shared__ uint64_t acc[8];
@@ -83,25 +102,15 @@ __device__ void finish_msg_body(const uint64_t *partials, int n, uint64_t *out) 
         acc[threadIdx.x] = x;
     }
     __syncthreads();
-    if (threadIdx.x == 0) {
-        gf_wide w0, w2;
-        for (int i = 0; i < 4; ++i) {
-            w0.w[i] = acc[i];
-            w2.w[i] = acc[4 + i];
-        }
-        const uint4 u0 = gf_reduce(w0), u2 = gf_reduce(w2);
-        out[0] = lo64(u0);
-        out[1] = hi64(u0);
-        out[2] = lo64(u2);
-        out[3] = hi64(u2);
-    }
+    if (threadIdx.x == 0) store_msg(acc, out);
 }
 
 // The last CTA of a launch (the one whose ticket completes the count)
 // reduces every CTA's partials and posts {u0, u2} to a mailbox in mapped host
-// memory: the four words, then (after a system-scope fence) the sequence
-// number the host waits for.  It resets the ticket for the next launch.
-// Without a mailbox (ticket null) the caller launches finish_msg_kernel.
+// memory: the four words, then (a system-scope release store by the same
+// thread) the sequence number the host waits for.  It resets the ticket for
+// the next launch.  Without a mailbox (ticket null) the caller launches
+// finish_msg_kernel.
 struct MsgMailbox {
     unsigned int *ticket = nullptr;  // device counter, 0 between launches
     uint64_t *words = nullptr;       // mapped host memory: u0, u2
@@ -120,10 +129,83 @@ __device__ void msg_epilogue(const uint64_t *partials, const MsgMailbox &mb) {
     __threadfence();
     finish_msg_body(partials, (int)gridDim.x, mb.words);
     if (threadIdx.x == 0) {
-        __threadfence_system();
-        *reinterpret_cast<volatile uint32_t *>(mb.seq) = mb.seq_val;
+        st_release_sys(mb.seq, mb.seq_val);
         *mb.ticket = 0;
     }
+}
+
+// A single-CTA launch with a mailbox reduces its terms in shared memory and
+// posts them itself (no partials, no ticket); otherwise every CTA stores its
+// partial and the last one posts.
+__device__ __forceinline__ void msg_finish(gf_wide u0, gf_wide u2, uint64_t *partials,
+                                           const MsgMailbox &mb) {
+    if (mb.ticket && gridDim.x == 1) {
+        __shared__ uint64_t acc[8];
+        cta_store_pair(u0, u2, acc);
+        __syncthreads();
+        if (threadIdx.x == 0) {
+            store_msg(acc, mb.words);
+            st_release_sys(mb.seq, mb.seq_val);
+        }
+        return;
+    }
+    cta_store_pair(u0, u2, partials + (uint64_t)blockIdx.x * 8);
+    msg_epilogue(partials, mb);
+}
+
+// Out of line for the fold kernel: its loop runs at the 128-register cap, and
+// an inlined epilogue adds spills to it.
+__device__ __noinline__ void msg_finish_call(gf_wide u0, gf_wide u2, uint64_t *partials,
+                                             const MsgMailbox &mb) {
+    msg_finish(u0, u2, partials, mb);
+}
+
+__device__ __forceinline__ uint32_t ld_acquire_sys(const uint32_t *p) {
+    uint32_t v;
+    asm volatile("ld.acquire.sys.global.u32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
+    return v;
+}
+
+__device__ __forceinline__ uint64_t globaltimer_ns() {
+    uint64_t t;
+    asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+    return t;
+}
+
+// Thread 0 of each CTA polls the gate word, sleeping between polls, until it
+// reads the round's sequence number (open: r is read behind it), the number
+// with bit 31 set (cancelled) or the time limit passes (the round is recorded
+// in *err).  Returns whether the gate opened; r is then the posted challenge.
+__device__ bool gate_wait(const RGate &g, uint4 &r) {
+    __shared__ uint4 rs;
+    __shared__ int open;
+    if (threadIdx.x == 0) {
+        const uint64_t t0 = globaltimer_ns();
+        int st = 0;
+        for (;;) {
+            const uint32_t v = ld_acquire_sys(g.go);
+            if (v == g.seq) {
+                st = 1;
+                break;
+            }
+            if (v == (g.seq | kGateCancel)) break;
+            if (globaltimer_ns() - t0 > kGateLimitNs) {
+                atomicExch(g.err, g.seq);
+                break;
+            }
+            __nanosleep(128);
+        }
+        if (st) {
+            const volatile uint64_t *rp = g.r;
+            const uint64_t lo = rp[0], hi = rp[1];
+            rs = make_uint4((uint32_t)lo, (uint32_t)(lo >> 32), (uint32_t)hi,
+                            (uint32_t)(hi >> 32));
+        }
+        open = st;
+    }
+    __syncthreads();
+    r = rs;
+    return open != 0;
 }
 
 // nf[j] = f[2j] + (f[2j] + f[2j+1]) * r (same for b); thread k produces the
@@ -132,11 +214,18 @@ __device__ void msg_epilogue(const uint64_t *partials, const MsgMailbox &mb) {
 // use the generic carry-less multiply.  Registers are capped at 128 so two
 // CTAs share an SM (a few spilled words cost less than half the warps: the
 // 2^24 first fold takes 0.30 ms instead of 0.35 ms).
+// GATED: launched before r is known; r comes through the gate instead (a
+// cancelled or timed-out CTA returns before touching the arrays or the
+// mailbox ticket).
+template <bool GATED>
 __global__ void __launch_bounds__(256, 2) fold_and_msg_kernel(const uint4 *f, const uint4 *b,
                                                            uint64_t half, uint4 r, uint4 *nf,
                                                            uint4 *nb, uint64_t *partials,
-                                                           MsgMailbox mb) {
+                                                           MsgMailbox mb, RGate gate) {
     extern __shared__ uint4 smem[];
+    if constexpr (GATED) {
+        if (!gate_wait(gate, r)) return;
+    }
     const char *T = build_r_table(smem, r);
     T16Lane8 lc;
     lc.init();
@@ -162,8 +251,7 @@ __global__ void __launch_bounds__(256, 2) fold_and_msg_kernel(const uint4 *f, co
         nf[0] = gf_add(f[0], gf_mul(gf_add(f[0], f[1]), r));
         nb[0] = gf_add(b[0], gf_mul(gf_add(b[0], b[1]), r));
     }
-    cta_store_pair(u0, u2, partials + (uint64_t)blockIdx.x * 8);
-    msg_epilogue(partials, mb);
+    msg_finish_call(u0, u2, partials, mb);
 }
 
 __global__ void __launch_bounds__(256) round_msg_kernel(const uint4 *f, const uint4 *b,
@@ -176,8 +264,7 @@ __global__ void __launch_bounds__(256) round_msg_kernel(const uint4 *f, const ui
         gf_wide_xor(u0, gf_mul_wide(f0, b0));
         gf_wide_xor(u2, gf_mul_wide(gf_add(f0, f1), gf_add(b0, b1)));
     }
-    cta_store_pair(u0, u2, partials + (uint64_t)blockIdx.x * 8);
-    msg_epilogue(partials, mb);
+    msg_finish(u0, u2, partials, mb);
 }
 
 // Final XOR of per-CTA partials and the single reduction: out = {u0, u2}.
@@ -196,15 +283,21 @@ size_t fold_partials_bytes(size_t n) {
     return (size_t)1024 * 8 * sizeof(uint64_t);  // up to 1024 CTAs
 }
 
+int fold_grid(size_t n, int num_sms) { return std::min(msg_grid(n / 4, num_sms), 1024); }
+
 int launch_fold_and_msg(const uint4 *d_f, const uint4 *d_b, size_t n, uint4 r, uint4 *d_nf,
                         uint4 *d_nb, uint64_t *d_partials, uint64_t *d_msg_out, cudaStream_t st,
-                        int num_sms, const MsgPost *post) {
+                        int num_sms, const MsgPost *post, const RGate *gate) {
     const uint64_t half = n / 2;
-    const int grid = std::min(msg_grid(half / 2, num_sms), 1024);
+    const int grid = fold_grid(n, num_sms);
     MsgMailbox mb;
     if (post) mb = {post->ticket, post->words, post->seq, post->seq_val};
-    fold_and_msg_kernel<<<grid, 256, kRTableSmem, st>>>(d_f, d_b, half, r, d_nf, d_nb, d_partials,
-                                                         mb);
+    if (gate)
+        fold_and_msg_kernel<true><<<grid, 256, kRTableSmem, st>>>(d_f, d_b, half, r, d_nf, d_nb,
+                                                                  d_partials, mb, *gate);
+    else
+        fold_and_msg_kernel<false><<<grid, 256, kRTableSmem, st>>>(d_f, d_b, half, r, d_nf, d_nb,
+                                                                   d_partials, mb, RGate{});
     if (post) return 1;
     finish_msg_kernel<<<1, kFinishThreads, 0, st>>>(d_partials, grid, d_msg_out);
     return 2;
@@ -385,7 +478,9 @@ __global__ void __launch_bounds__(256) phi_kernel(const uint4 *eq_hi, uint64_t n
 
 void init_fold_kernels() {
     cudaFuncSetAttribute(phi_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, 65536);
-    cudaFuncSetAttribute(fold_and_msg_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+    cudaFuncSetAttribute(fold_and_msg_kernel<false>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                         (int)kRTableSmem);
+    cudaFuncSetAttribute(fold_and_msg_kernel<true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                          (int)kRTableSmem);
     cudaFuncSetAttribute(partial_eval_round_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
                          (int)kRTableSmem);

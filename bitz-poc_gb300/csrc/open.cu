@@ -76,6 +76,7 @@ struct Sumcheck {
     size_t len = 0;
     bool next_in_B = false;       // where the next fold writes
     std::vector<uint64_t> msgs;   // 4 words per SumcheckMessage
+    bz::ArmedFold armed;          // the next round's fold, enqueued ahead of its challenge
 
     const uint64_t *basis() const { return b ? b : b_in; }
 
@@ -101,6 +102,10 @@ struct Sumcheck {
     }
 
     void release() {
+        if (armed.live) {
+            bz::fold_cancel(ctx, &armed);
+            bz::reset_msg_ticket(ctx);
+        }
         if (buf) bz::dev_free(ctx, buf, buf_bytes, false);
         buf = nullptr;
     }
@@ -114,9 +119,14 @@ struct Sumcheck {
         return BZ_OK;
     }
 
-    // one fold round: optional grind, challenge, fold, observe
-    int fold_round(uint32_t bits, std::vector<uint64_t> &fold_nonces, uint64_t r_out[2]) {
+    // one fold round: optional grind, challenge, fold, observe.  With
+    // arm_next (the caller's next step is another fold round without a
+    // grind), the next round's fold is enqueued before this round's message
+    // is read, so its launch overlaps the host's wait and transcript work.
+    int fold_round(uint32_t bits, std::vector<uint64_t> &fold_nonces, uint64_t r_out[2],
+                   bool arm_next = false) {
         if (bits) {
+            if (armed.live) return bz::set_msg(ctx, BZ_ERR_STATE, "grind behind an armed fold");
             uint64_t nonce;
             int rc = bz_transcript_grind_pow(ctx, transcript, bits, &nonce);
             if (rc) return rc;
@@ -125,14 +135,36 @@ struct Sumcheck {
         tr->sample_f128(r_out);
         uint4 *dst = next_in_B ? B : A;
         uint64_t *nf = (uint64_t *)dst, *nb = (uint64_t *)(dst + len / 2);
-        uint64_t u0[2], u2[2];
-        int rc = bz_fold_and_msg_lsb(ctx, f, basis(), len, r_out, nf, nb, u0, u2);
-        if (rc) return rc;
-        record(u0, u2);
+        uint32_t seq = 0;
+        int rc = BZ_OK;
+        if (armed.live) {
+            if (armed.f != f || armed.b != basis() || armed.n != len || armed.nf != nf ||
+                armed.nb != nb) {
+                bz::fold_cancel(ctx, &armed);
+                bz::reset_msg_ticket(ctx);
+                return bz::set_msg(ctx, BZ_ERR_STATE, "armed fold does not match the round");
+            }
+            seq = armed.msg_seq;
+            bz::fold_open(ctx, &armed, r_out);
+        } else if ((rc = bz::fold_launch(ctx, f, basis(), len, r_out, nf, nb, &seq))) {
+            return rc;
+        }
         f = nf;
         b = nb;
         len /= 2;
         next_in_B = !next_in_B;
+        if (arm_next && bz::fold_armable(ctx, len)) {
+            uint4 *nd = next_in_B ? B : A;
+            rc = bz::fold_arm(ctx, f, b, len, (uint64_t *)nd, (uint64_t *)(nd + len / 2), &armed);
+        }
+        uint64_t u0[2], u2[2];
+        const int wrc = bz::msg_wait(ctx, seq, u0, u2);
+        if (rc || wrc) {
+            if (armed.live) bz::fold_cancel(ctx, &armed);
+            bz::reset_msg_ticket(ctx);
+            return rc ? rc : wrc;
+        }
+        record(u0, u2);
         return BZ_OK;
     }
 
@@ -372,8 +404,9 @@ int open_level0(bz_ctx *ctx, bz_transcript *transcript, bz_commitment *c0,
     if ((rc = o->sc.first_message())) return fail(rc);
     for (uint32_t j = 0; j < k; ++j) {
         const uint32_t bits = cfg->fold_grinding_bits0 > j ? cfg->fold_grinding_bits0 - j : 0;
+        const bool arm = j + 1 < k && cfg->fold_grinding_bits0 <= j + 1;
         uint64_t r[2];
-        if ((rc = o->sc.fold_round(bits, o->fold_nonces, r))) return fail(rc);
+        if ((rc = o->sc.fold_round(bits, o->fold_nonces, r, arm))) return fail(rc);
         o->challenges.insert(o->challenges.end(), {r[0], r[1]});
     }
 
@@ -542,8 +575,9 @@ int bz_ligerito_prove(bz_ctx *ctx, bz_transcript *transcript, bz_commitment *c0,
         const uint32_t prev_rate = cfg->log_inv_rates[i + 1];
         for (uint32_t j = 0; j < cfg->recursive_ks[i]; ++j) {
             const uint32_t bits = fold_bits(i + 1) > j ? fold_bits(i + 1) - j : 0;
+            const bool arm = j + 1 < cfg->recursive_ks[i] && fold_bits(i + 1) <= j + 1;
             uint64_t ri[2];
-            if ((rc = sc.fold_round(bits, p->fold_grinding_nonces, ri))) return finish(rc);
+            if ((rc = sc.fold_round(bits, p->fold_grinding_nonces, ri, arm))) return finish(rc);
         }
         const uint64_t block_len = prev->shape.n_leaves();
         if (i == r - 1) {

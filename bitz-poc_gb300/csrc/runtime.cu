@@ -829,6 +829,10 @@ static uint4 to_u4(const uint64_t r[2]) {
 
 static bool pow2(size_t n) { return n && !(n & (n - 1)); }
 
+}  // extern "C"
+
+namespace bz {
+
 // Mailbox post for the next message kernel on the context stream.
 static MsgPost next_post(bz_ctx *ctx) {
     MsgPost p;
@@ -840,11 +844,15 @@ static MsgPost next_post(bz_ctx *ctx) {
     return p;
 }
 
+void reset_msg_ticket(bz_ctx *ctx) {
+    cudaMemsetAsync((uint8_t *)ctx->d_small + 768, 0, 4, ctx->stream);
+}
+
 // Wait for the message kernel to post sequence number seq, then read
 // {u0, u2}.  The wait spins on the mailbox (no stream synchronisation on the
 // critical path), checking the stream every few hundred spins so that a
 // failed launch returns its error, and gives up after 60 s.
-static int wait_msg(bz_ctx *ctx, uint32_t seq, uint64_t u0[2], uint64_t u2[2]) {
+int msg_wait(bz_ctx *ctx, uint32_t seq, uint64_t u0[2], uint64_t u2[2]) {
     volatile uint32_t *sp = (volatile uint32_t *)((uint8_t *)ctx->h_mbox + 64);
     const auto t0 = std::chrono::steady_clock::now();
     for (uint64_t spin = 1; *sp != seq; ++spin) {
@@ -871,11 +879,8 @@ static int wait_msg(bz_ctx *ctx, uint32_t seq, uint64_t u0[2], uint64_t u2[2]) {
     return BZ_OK;
 }
 
-int bz_fold_and_msg_lsb(bz_ctx *ctx, const uint64_t *d_f, const uint64_t *d_b, size_t n,
-                        const uint64_t r[2], uint64_t *d_nf, uint64_t *d_nb, uint64_t u0[2],
-                        uint64_t u2[2]) {
-    if (!ctx || !d_f || !d_b || !r || !d_nf || !d_nb) return BZ_ERR_ARG;
-    if (!pow2(n) || n < 2) return set_msg(ctx, BZ_ERR_SHAPE, "n must be a power of two >= 2");
+int fold_launch(bz_ctx *ctx, const uint64_t *d_f, const uint64_t *d_b, size_t n,
+                const uint64_t r[2], uint64_t *d_nf, uint64_t *d_nb, uint32_t *msg_seq) {
     int rc = ensure_scratch(ctx, fold_partials_bytes(n));
     if (rc) return rc;
     const MsgPost post = next_post(ctx);
@@ -883,7 +888,81 @@ int bz_fold_and_msg_lsb(bz_ctx *ctx, const uint64_t *d_f, const uint64_t *d_b, s
                                          (uint4 *)d_nf, (uint4 *)d_nb, (uint64_t *)ctx->scratch,
                                          nullptr, ctx->stream, ctx->num_sms, &post);
     BZ_CUDA(ctx, cudaGetLastError());
-    return wait_msg(ctx, post.seq_val, u0, u2);
+    *msg_seq = post.seq_val;
+    return BZ_OK;
+}
+
+// The gate: r at byte 128 and the go word at byte 192 of the mapped mailbox;
+// the kernel's time-out record at byte 832 of the small device buffer.
+static uint8_t *gate_host(bz_ctx *ctx) { return (uint8_t *)ctx->h_mbox + 128; }
+
+// Armed only while every CTA of the fold fits on the GPU at once, so that
+// the CTAs that wait at the gate are few.
+bool fold_armable(const bz_ctx *ctx, size_t n) {
+    return n >= 2 && fold_grid(n, ctx->num_sms) <= 2 * ctx->num_sms;
+}
+
+int fold_arm(bz_ctx *ctx, const uint64_t *d_f, const uint64_t *d_b, size_t n, uint64_t *d_nf,
+             uint64_t *d_nb, ArmedFold *a) {
+    if (a->live) return set_msg(ctx, BZ_ERR_STATE, "a fold is already armed");
+    int rc = ensure_scratch(ctx, fold_partials_bytes(n));
+    if (rc) return rc;
+    if (++ctx->gate_seq >= kGateCancel) ctx->gate_seq = 1;
+    RGate g;
+    g.r = (const uint64_t *)((uint8_t *)ctx->d_mbox + 128);
+    g.go = (const uint32_t *)((uint8_t *)ctx->d_mbox + 192);
+    g.seq = ctx->gate_seq;
+    g.err = (uint32_t *)((uint8_t *)ctx->d_small + 832);
+    const MsgPost post = next_post(ctx);
+    ctx->launches += launch_fold_and_msg((const uint4 *)d_f, (const uint4 *)d_b, n,
+                                         make_uint4(0, 0, 0, 0), (uint4 *)d_nf, (uint4 *)d_nb,
+                                         (uint64_t *)ctx->scratch, nullptr, ctx->stream,
+                                         ctx->num_sms, &post, &g);
+    BZ_CUDA(ctx, cudaGetLastError());
+    a->gate_seq = g.seq;
+    a->msg_seq = post.seq_val;
+    a->f = d_f;
+    a->b = d_b;
+    a->nf = d_nf;
+    a->nb = d_nb;
+    a->n = n;
+    a->live = true;
+    return BZ_OK;
+}
+
+// r first, then (release) the go word.
+void fold_open(bz_ctx *ctx, ArmedFold *a, const uint64_t r[2]) {
+    uint64_t *hr = (uint64_t *)gate_host(ctx);
+    __atomic_store_n(&hr[0], r[0], __ATOMIC_RELAXED);
+    __atomic_store_n(&hr[1], r[1], __ATOMIC_RELAXED);
+    __atomic_store_n((uint32_t *)(gate_host(ctx) + 64), a->gate_seq, __ATOMIC_RELEASE);
+    a->live = false;
+}
+
+// The cancelled CTAs return before touching the arrays or the ticket; the
+// stream is drained so that nothing armed outlives the call.
+int fold_cancel(bz_ctx *ctx, ArmedFold *a) {
+    if (!a->live) return BZ_OK;
+    __atomic_store_n((uint32_t *)(gate_host(ctx) + 64), a->gate_seq | kGateCancel,
+                     __ATOMIC_RELEASE);
+    a->live = false;
+    BZ_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+    return BZ_OK;
+}
+
+}  // namespace bz
+
+extern "C" {
+
+int bz_fold_and_msg_lsb(bz_ctx *ctx, const uint64_t *d_f, const uint64_t *d_b, size_t n,
+                        const uint64_t r[2], uint64_t *d_nf, uint64_t *d_nb, uint64_t u0[2],
+                        uint64_t u2[2]) {
+    if (!ctx || !d_f || !d_b || !r || !d_nf || !d_nb) return BZ_ERR_ARG;
+    if (!pow2(n) || n < 2) return set_msg(ctx, BZ_ERR_SHAPE, "n must be a power of two >= 2");
+    uint32_t seq = 0;
+    int rc = fold_launch(ctx, d_f, d_b, n, r, d_nf, d_nb, &seq);
+    if (rc) return rc;
+    return msg_wait(ctx, seq, u0, u2);
 }
 
 int bz_round_msg_lsb(bz_ctx *ctx, const uint64_t *d_f, const uint64_t *d_b, size_t n,
@@ -897,7 +976,7 @@ int bz_round_msg_lsb(bz_ctx *ctx, const uint64_t *d_f, const uint64_t *d_b, size
                                       (uint64_t *)ctx->scratch, nullptr, ctx->stream, ctx->num_sms,
                                       &post);
     BZ_CUDA(ctx, cudaGetLastError());
-    return wait_msg(ctx, post.seq_val, u0, u2);
+    return msg_wait(ctx, post.seq_val, u0, u2);
 }
 
 int bz_partial_eval_lsb(bz_ctx *ctx, const uint64_t *d_in, size_t n, const uint64_t *rs, size_t k,

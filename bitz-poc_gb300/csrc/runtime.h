@@ -55,6 +55,7 @@ struct bz_ctx {
     void *h_mbox = nullptr;   // 4 KiB mapped pinned: sumcheck message mailbox
     void *d_mbox = nullptr;   // its device view
     uint32_t mbox_seq = 0;    // last posted sequence number
+    uint32_t gate_seq = 0;    // last armed fold's gate number
     cudaEvent_t ev0 = nullptr, ev1 = nullptr;
     std::mutex aux_mu;
     std::map<cudaStream_t, bz_aux_stream> aux;
@@ -111,4 +112,30 @@ bz_aux_stream *get_aux(bz_ctx *ctx, cudaStream_t st);
 int launch_commit_kernels(bz_ctx *ctx, const Shape &s, uint32_t schedule, const uint4 *d_msg,
                           uint4 *d_cw, uint8_t *d_tree, const uint4 *d_tw, cudaStream_t st,
                           LaunchLog *log);
+
+// Sumcheck rounds on the context stream.  fold_launch enqueues one
+// fold-and-message round with a known challenge; msg_wait returns its
+// message.  A fold can also be armed: enqueued before its challenge exists,
+// behind the round in flight, so that its launch overlaps the host's wait and
+// transcript work; fold_open posts the challenge, fold_cancel withdraws it.
+// Between fold_arm and fold_open/fold_cancel the host must not wait on the
+// context stream (the armed kernel would hold it until its time limit).
+struct ArmedFold {
+    uint32_t gate_seq = 0;
+    uint32_t msg_seq = 0;
+    const uint64_t *f = nullptr, *b = nullptr;
+    uint64_t *nf = nullptr, *nb = nullptr;
+    size_t n = 0;
+    bool live = false;
+};
+int fold_launch(bz_ctx *ctx, const uint64_t *d_f, const uint64_t *d_b, size_t n,
+                const uint64_t r[2], uint64_t *d_nf, uint64_t *d_nb, uint32_t *msg_seq);
+bool fold_armable(const bz_ctx *ctx, size_t n);
+int fold_arm(bz_ctx *ctx, const uint64_t *d_f, const uint64_t *d_b, size_t n, uint64_t *d_nf,
+             uint64_t *d_nb, ArmedFold *a);
+void fold_open(bz_ctx *ctx, ArmedFold *a, const uint64_t r[2]);
+int fold_cancel(bz_ctx *ctx, ArmedFold *a);
+int msg_wait(bz_ctx *ctx, uint32_t seq, uint64_t u0[2], uint64_t u2[2]);
+// Zero the message ticket (after a round that may have stopped part-way).
+void reset_msg_ticket(bz_ctx *ctx);
 }  // namespace bz
