@@ -71,6 +71,7 @@ _SIGS = {
     "bz_fold_and_msg_lsb": (_I, [_P, _P, _P, _S, _P, _P, _P, _P, _P]),
     "bz_fold_and_msg_lsb_static": (_I, [_P, _P, _S, _P, _P, _P, _P, _P]),
     "bz_round_msg_lsb": (_I, [_P, _P, _P, _S, _P, _P]),
+    "bz_fold_gate_check": (_I, [_P, _P, _P, _S, _P, _P, _P, _I, _U64, _P, _P]),
     "bz_partial_eval_lsb": (_I, [_P, _P, _S, _P, _S, _P]),
     "bz_build_eq_lsb": (_I, [_P, _P, _S, _P]),
     "bz_sv_fold": (_I, [_P, _P, _P, _S, _P]),

@@ -49,6 +49,26 @@ def fold_and_msg_lsb(f: DeviceArray, b: DeviceArray, r, ctx: Context | None = No
     return nf, nb, (u0, u2)
 
 
+def fold_gate_check(f: DeviceArray, b: DeviceArray, r, mode: int, limit_ns: int = 0,
+                    ctx: Context | None = None):
+    """The armed fold that the prover uses for its small rounds, driven by
+    hand (bz_fold_gate_check): mode 0 posts r and returns (folded f, folded b,
+    (u0, u2)) like fold_and_msg_lsb; mode 1 cancels the round; mode 2 posts
+    nothing and raises BzError(BZ_ERR_TIMEOUT) once the kernel's bounded wait
+    has run out."""
+    ctx = ctx or f.ctx
+    if f.n != b.n:
+        raise ValueError("f and b lengths differ")
+    nf = DeviceArray(f.n // 2, ctx)
+    nb = DeviceArray(f.n // 2, ctx)
+    u0 = np.zeros(2, np.uint64)
+    u2 = np.zeros(2, np.uint64)
+    check(ctx.handle, lib().bz_fold_gate_check(ctx.handle, f.ptr, b.ptr, f.n, ptr(_gf(r)),
+                                               nf.ptr, nb.ptr, mode, limit_ns, ptr(u0),
+                                               ptr(u2)))
+    return nf, nb, (u0, u2)
+
+
 def partial_eval_lsb(evals: DeviceArray, rs, ctx: Context | None = None) -> DeviceArray:
     ctx = ctx or evals.ctx
     r = np.ascontiguousarray(np.asarray(rs, dtype=np.uint64).reshape(-1, 2))

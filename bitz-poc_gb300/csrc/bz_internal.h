@@ -122,7 +122,7 @@ struct MsgPost {
 };
 // Challenge gate of a fold launched ahead of its challenge: the host writes r
 // to mapped memory, then the sequence number to `go` (or seq | kGateCancel to
-// cancel).  The kernel waits at most kGateLimitNs, then records seq in *err.
+// cancel).  The kernel waits at most limit_ns, then records seq in *err.
 constexpr uint32_t kGateCancel = 0x80000000u;
 constexpr uint64_t kGateLimitNs = 5000000000ull;
 struct RGate {
@@ -130,6 +130,7 @@ struct RGate {
     const uint64_t *r = nullptr;   // device view of mapped host memory: r.lo, r.hi
     uint32_t seq = 0;              // 1 .. kGateCancel - 1
     uint32_t *err = nullptr;       // device memory
+    uint64_t limit_ns = kGateLimitNs;
 };
 size_t fold_partials_bytes(size_t n);
 int fold_grid(size_t n, int num_sms);

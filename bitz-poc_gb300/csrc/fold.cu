@@ -189,7 +189,7 @@ __device__ bool gate_wait(const RGate &g, uint4 &r) {
                 break;
             }
             if (v == (g.seq | kGateCancel)) break;
-            if (globaltimer_ns() - t0 > kGateLimitNs) {
+            if (globaltimer_ns() - t0 > g.limit_ns) {
                 atomicExch(g.err, g.seq);
                 break;
             }

@@ -903,7 +903,7 @@ bool fold_armable(const bz_ctx *ctx, size_t n) {
 }
 
 int fold_arm(bz_ctx *ctx, const uint64_t *d_f, const uint64_t *d_b, size_t n, uint64_t *d_nf,
-             uint64_t *d_nb, ArmedFold *a) {
+             uint64_t *d_nb, ArmedFold *a, uint64_t limit_ns) {
     if (a->live) return set_msg(ctx, BZ_ERR_STATE, "a fold is already armed");
     int rc = ensure_scratch(ctx, fold_partials_bytes(n));
     if (rc) return rc;
@@ -913,6 +913,7 @@ int fold_arm(bz_ctx *ctx, const uint64_t *d_f, const uint64_t *d_b, size_t n, ui
     g.go = (const uint32_t *)((uint8_t *)ctx->d_mbox + 192);
     g.seq = ctx->gate_seq;
     g.err = (uint32_t *)((uint8_t *)ctx->d_small + 832);
+    g.limit_ns = limit_ns;
     const MsgPost post = next_post(ctx);
     ctx->launches += launch_fold_and_msg((const uint4 *)d_f, (const uint4 *)d_b, n,
                                          make_uint4(0, 0, 0, 0), (uint4 *)d_nf, (uint4 *)d_nb,
@@ -963,6 +964,33 @@ int bz_fold_and_msg_lsb(bz_ctx *ctx, const uint64_t *d_f, const uint64_t *d_b, s
     int rc = fold_launch(ctx, d_f, d_b, n, r, d_nf, d_nb, &seq);
     if (rc) return rc;
     return msg_wait(ctx, seq, u0, u2);
+}
+
+int bz_fold_gate_check(bz_ctx *ctx, const uint64_t *d_f, const uint64_t *d_b, size_t n,
+                       const uint64_t r[2], uint64_t *d_nf, uint64_t *d_nb, int mode,
+                       uint64_t limit_ns, uint64_t u0[2], uint64_t u2[2]) {
+    if (!ctx || !d_f || !d_b || !d_nf || !d_nb || mode < 0 || mode > 2 || (mode == 0 && !r))
+        return BZ_ERR_ARG;
+    if (!pow2(n) || n < 2) return set_msg(ctx, BZ_ERR_SHAPE, "n must be a power of two >= 2");
+    ArmedFold a;
+    int rc = fold_arm(ctx, d_f, d_b, n, d_nf, d_nb, &a, limit_ns ? limit_ns : kGateLimitNs);
+    if (rc) return rc;
+    if (mode == 0) {
+        fold_open(ctx, &a, r);
+        return msg_wait(ctx, a.msg_seq, u0, u2);
+    }
+    if (mode == 1) return fold_cancel(ctx, &a);
+    // mode 2: nothing is posted; the kernel's CTAs give up at the time limit
+    a.live = false;
+    BZ_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+    uint32_t *d_err = (uint32_t *)((uint8_t *)ctx->d_small + 832);
+    uint32_t err = 0;
+    BZ_CUDA(ctx, cudaMemcpy(&err, d_err, 4, cudaMemcpyDeviceToHost));
+    BZ_CUDA(ctx, cudaMemset(d_err, 0, 4));
+    reset_msg_ticket(ctx);
+    BZ_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+    if (err != a.gate_seq) return set_msg(ctx, BZ_ERR_STATE, "the gate did not record its time-out");
+    return set_msg(ctx, BZ_ERR_TIMEOUT, "fold gate: no challenge posted within the limit");
 }
 
 int bz_round_msg_lsb(bz_ctx *ctx, const uint64_t *d_f, const uint64_t *d_b, size_t n,

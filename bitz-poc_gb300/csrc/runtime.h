@@ -132,7 +132,7 @@ int fold_launch(bz_ctx *ctx, const uint64_t *d_f, const uint64_t *d_b, size_t n,
                 const uint64_t r[2], uint64_t *d_nf, uint64_t *d_nb, uint32_t *msg_seq);
 bool fold_armable(const bz_ctx *ctx, size_t n);
 int fold_arm(bz_ctx *ctx, const uint64_t *d_f, const uint64_t *d_b, size_t n, uint64_t *d_nf,
-             uint64_t *d_nb, ArmedFold *a);
+             uint64_t *d_nb, ArmedFold *a, uint64_t limit_ns = kGateLimitNs);
 void fold_open(bz_ctx *ctx, ArmedFold *a, const uint64_t r[2]);
 int fold_cancel(bz_ctx *ctx, ArmedFold *a);
 int msg_wait(bz_ctx *ctx, uint32_t seq, uint64_t u0[2], uint64_t u2[2]);

@@ -263,6 +263,19 @@ int bz_fold_and_msg_lsb_static(const uint64_t *d_f, const uint64_t *d_b, size_t 
 /* round_msg_lsb (ligerito.rs:2500-2537). */
 int bz_round_msg_lsb(bz_ctx *ctx, const uint64_t *d_f, const uint64_t *d_b, size_t n,
                      uint64_t u0[2], uint64_t u2[2]);
+/* Check of the armed fold that the prover uses for its small rounds (no
+ * counterpart in the reference).  The prover enqueues such a round before its
+ * challenge exists; the kernel waits at its gate, for at most limit_ns (0 =
+ * the prover's 5 s), until the host posts r.  This call arms one
+ * bz_fold_and_msg_lsb round of length n, then:
+ *   mode 0: posts r and returns the round's message (as bz_fold_and_msg_lsb);
+ *   mode 1: cancels it (BZ_OK, nothing written);
+ *   mode 2: posts nothing, waits for the kernel to give up and returns
+ *           BZ_ERR_TIMEOUT.
+ * Every mode leaves the context ready for further rounds. */
+int bz_fold_gate_check(bz_ctx *ctx, const uint64_t *d_f, const uint64_t *d_b, size_t n,
+                       const uint64_t r[2], uint64_t *d_nf, uint64_t *d_nb, int mode,
+                       uint64_t limit_ns, uint64_t u0[2], uint64_t u2[2]);
 /* partial_eval_lsb (ligerito.rs:1678-1695): fold the k LSB variables by
  * rs[0..k) (host array of k elements); d_out holds n >> k elements. */
 int bz_partial_eval_lsb(bz_ctx *ctx, const uint64_t *d_in, size_t n, const uint64_t *rs,

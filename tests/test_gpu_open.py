@@ -53,6 +53,34 @@ def test_fold_and_msg(oracle, ctx, n):
     assert (m0 == o0).all() and (m2 == o2).all()
 
 
+@pytest.mark.parametrize("n", [2, 64, 1 << 12, 1 << 16])
+def test_armed_fold_gate(oracle, ctx, n):
+    """The armed fold of the prover's small rounds: opened it equals the
+    oracle's fold; cancelled it writes nothing; left without a challenge its
+    bounded wait runs out (a gate that nothing opens) and the context keeps
+    working."""
+    from bitz_gb300 import DeviceArray
+    from bitz_gb300._lib import BzError
+    from bitz_gb300.ligerito import fold_and_msg_lsb, fold_gate_check
+
+    rng = np.random.default_rng(n + 5)
+    f, b, r = _rand(rng, n), _rand(rng, n), _rand(rng, 1)[0]
+    df, db = DeviceArray.from_host(f, ctx), DeviceArray.from_host(b, ctx)
+    ef, eb, e0, e2 = oracle.fold_and_msg_lsb(f, b, r)
+    nf, nb, (u0, u2) = fold_gate_check(df, db, r, 0)
+    assert (nf.to_host() == ef).all() and (nb.to_host() == eb).all()
+    assert (u0 == e0).all() and (u2 == e2).all()
+    fold_gate_check(df, db, r, 1)
+    with pytest.raises(BzError) as e:
+        fold_gate_check(df, db, r, 2, limit_ns=20_000_000)
+    assert e.value.status == 6  # BZ_ERR_TIMEOUT
+    for _ in range(2):
+        nf, nb, (u0, u2) = fold_and_msg_lsb(df, db, r)
+        assert (nf.to_host() == ef).all() and (u0 == e0).all() and (u2 == e2).all()
+        nf, nb, (u0, u2) = fold_gate_check(df, db, r, 0)
+        assert (nb.to_host() == eb).all() and (u0 == e0).all() and (u2 == e2).all()
+
+
 def test_sumcheck_prover_chain(oracle, ctx):
     """SumcheckProver.new + k folds (the initial_k L0 loop of
     ligerito.rs:3621-3657) against the oracle's chain."""
