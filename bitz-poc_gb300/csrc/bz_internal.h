@@ -122,9 +122,12 @@ struct MsgPost {
 };
 // Challenge gate of a fold launched ahead of its challenge: the host writes r
 // to mapped memory, then the sequence number to `go` (or seq | kGateCancel to
-// cancel).  The kernel waits at most limit_ns, then records seq in *err.
+// cancel).  The kernel waits at most limit_ns, then sets bit 0 of *err.  The
+// host posts r within microseconds; the limit only bounds a gate that nothing
+// opens (an error path, or a tool that runs each launch to completion before
+// returning), and the prover then runs the round again unarmed.
 constexpr uint32_t kGateCancel = 0x80000000u;
-constexpr uint64_t kGateLimitNs = 5000000000ull;
+constexpr uint64_t kGateLimitNs = 100000000ull;  // 100 ms
 struct RGate {
     const uint32_t *go = nullptr;  // device view of mapped host memory
     const uint64_t *r = nullptr;   // device view of mapped host memory: r.lo, r.hi

@@ -174,8 +174,8 @@ __device__ __forceinline__ uint64_t globaltimer_ns() {
 
 // Thread 0 of each CTA polls the gate word, sleeping between polls, until it
 // reads the round's sequence number (open: r is read behind it), the number
-// with bit 31 set (cancelled) or the time limit passes (the round is recorded
-// in *err).  Returns whether the gate opened; r is then the posted challenge.
+// with bit 31 set (cancelled) or the time limit passes (bit 0 of *err is
+// set).  Returns whether the gate opened; r is then the posted challenge.
 __device__ bool gate_wait(const RGate &g, uint4 &r) {
     __shared__ uint4 rs;
     __shared__ int open;
@@ -190,7 +190,7 @@ __device__ bool gate_wait(const RGate &g, uint4 &r) {
             }
             if (v == (g.seq | kGateCancel)) break;
             if (globaltimer_ns() - t0 > g.limit_ns) {
-                atomicExch(g.err, g.seq);
+                atomicOr(g.err, 1u);
                 break;
             }
             __nanosleep(128);

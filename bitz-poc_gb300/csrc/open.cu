@@ -135,6 +135,9 @@ struct Sumcheck {
         tr->sample_f128(r_out);
         uint4 *dst = next_in_B ? B : A;
         uint64_t *nf = (uint64_t *)dst, *nb = (uint64_t *)(dst + len / 2);
+        const uint64_t *in_f = f, *in_b = basis();
+        const size_t in_len = len;
+        const bool was_armed = armed.live;
         uint32_t seq = 0;
         int rc = BZ_OK;
         if (armed.live) {
@@ -158,7 +161,17 @@ struct Sumcheck {
             rc = bz::fold_arm(ctx, f, b, len, (uint64_t *)nd, (uint64_t *)(nd + len / 2), &armed);
         }
         uint64_t u0[2], u2[2];
-        const int wrc = bz::msg_wait(ctx, seq, u0, u2);
+        int wrc = bz::msg_wait(ctx, seq, u0, u2);
+        if (wrc && was_armed && !rc) {
+            // the gate ran out before r arrived (a host stall, or a tool that
+            // completes each launch before returning): run the round unarmed
+            if (armed.live) bz::fold_cancel(ctx, &armed);
+            if (bz::gate_gave_up(ctx)) {
+                bz::reset_msg_ticket(ctx);
+                wrc = bz::fold_launch(ctx, in_f, in_b, in_len, r_out, nf, nb, &seq);
+                if (!wrc) wrc = bz::msg_wait(ctx, seq, u0, u2);
+            }
+        }
         if (rc || wrc) {
             if (armed.live) bz::fold_cancel(ctx, &armed);
             bz::reset_msg_ticket(ctx);

@@ -899,7 +899,18 @@ static uint8_t *gate_host(bz_ctx *ctx) { return (uint8_t *)ctx->h_mbox + 128; }
 // Armed only while every CTA of the fold fits on the GPU at once, so that
 // the CTAs that wait at the gate are few.
 bool fold_armable(const bz_ctx *ctx, size_t n) {
-    return n >= 2 && fold_grid(n, ctx->num_sms) <= 2 * ctx->num_sms;
+    return ctx->arm_folds && n >= 2 && fold_grid(n, ctx->num_sms) <= 2 * ctx->num_sms;
+}
+
+bool gate_gave_up(bz_ctx *ctx) {
+    uint32_t *d_err = (uint32_t *)((uint8_t *)ctx->d_small + 832);
+    uint32_t err = 0;
+    if (cudaStreamSynchronize(ctx->stream) != cudaSuccess ||
+        cudaMemcpy(&err, d_err, 4, cudaMemcpyDeviceToHost) != cudaSuccess || !err)
+        return false;
+    cudaMemset(d_err, 0, 4);
+    ctx->arm_folds = false;
+    return true;
 }
 
 int fold_arm(bz_ctx *ctx, const uint64_t *d_f, const uint64_t *d_b, size_t n, uint64_t *d_nf,
@@ -982,14 +993,12 @@ int bz_fold_gate_check(bz_ctx *ctx, const uint64_t *d_f, const uint64_t *d_b, si
     if (mode == 1) return fold_cancel(ctx, &a);
     // mode 2: nothing is posted; the kernel's CTAs give up at the time limit
     a.live = false;
-    BZ_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
-    uint32_t *d_err = (uint32_t *)((uint8_t *)ctx->d_small + 832);
-    uint32_t err = 0;
-    BZ_CUDA(ctx, cudaMemcpy(&err, d_err, 4, cudaMemcpyDeviceToHost));
-    BZ_CUDA(ctx, cudaMemset(d_err, 0, 4));
+    const bool arming = ctx->arm_folds;
+    const bool gave_up = gate_gave_up(ctx);
+    ctx->arm_folds = arming;  // a deliberate time-out: the prover's arming is unchanged
     reset_msg_ticket(ctx);
     BZ_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
-    if (err != a.gate_seq) return set_msg(ctx, BZ_ERR_STATE, "the gate did not record its time-out");
+    if (!gave_up) return set_msg(ctx, BZ_ERR_STATE, "the gate did not record its time-out");
     return set_msg(ctx, BZ_ERR_TIMEOUT, "fold gate: no challenge posted within the limit");
 }
 

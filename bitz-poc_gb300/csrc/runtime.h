@@ -56,6 +56,7 @@ struct bz_ctx {
     void *d_mbox = nullptr;   // its device view
     uint32_t mbox_seq = 0;    // last posted sequence number
     uint32_t gate_seq = 0;    // last armed fold's gate number
+    bool arm_folds = true;    // cleared after a gate ran out (the prover stops arming)
     cudaEvent_t ev0 = nullptr, ev1 = nullptr;
     std::mutex aux_mu;
     std::map<cudaStream_t, bz_aux_stream> aux;
@@ -135,6 +136,10 @@ int fold_arm(bz_ctx *ctx, const uint64_t *d_f, const uint64_t *d_b, size_t n, ui
              uint64_t *d_nb, ArmedFold *a, uint64_t limit_ns = kGateLimitNs);
 void fold_open(bz_ctx *ctx, ArmedFold *a, const uint64_t r[2]);
 int fold_cancel(bz_ctx *ctx, ArmedFold *a);
+// After a gated round's message failed to arrive: drains the stream and
+// reports (and clears) whether a gate ran out, which then stops arming on the
+// context.
+bool gate_gave_up(bz_ctx *ctx);
 int msg_wait(bz_ctx *ctx, uint32_t seq, uint64_t u0[2], uint64_t u2[2]);
 // Zero the message ticket (after a round that may have stopped part-way).
 void reset_msg_ticket(bz_ctx *ctx);

@@ -266,7 +266,7 @@ int bz_round_msg_lsb(bz_ctx *ctx, const uint64_t *d_f, const uint64_t *d_b, size
 /* Check of the armed fold that the prover uses for its small rounds (no
  * counterpart in the reference).  The prover enqueues such a round before its
  * challenge exists; the kernel waits at its gate, for at most limit_ns (0 =
- * the prover's 5 s), until the host posts r.  This call arms one
+ * the prover's 100 ms), until the host posts r.  This call arms one
  * bz_fold_and_msg_lsb round of length n, then:
  *   mode 0: posts r and returns the round's message (as bz_fold_and_msg_lsb);
  *   mode 1: cancels it (BZ_OK, nothing written);
