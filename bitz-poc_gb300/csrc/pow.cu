@@ -28,10 +28,21 @@
 namespace {
 
 constexpr int kPowThreads = 256;
-constexpr int kPowPerThread = 4;
-constexpr uint64_t kPowChunk = (uint64_t)kPowThreads * kPowPerThread;
+constexpr int kPowPerThread = 4;                    // nonces per thread per chunk above 20 bits
 constexpr uint64_t kPowWindow = (uint64_t)1 << 34;  // nonces per launch (< 1 s)
-constexpr size_t kPowCtlOffset = 256;               // bytes into the context's small buffers
+// Device state at this byte offset of the context's small buffer: the chunk
+// counter, the best hit and the blocks' exit ticket.  The launch's last block
+// posts the best hit to the mapped mailbox (kPowBestOffset, then the sequence
+// number at kPowSeqOffset) and restores the state for the next launch.
+constexpr size_t kPowCtlOffset = 256;
+constexpr size_t kPowBestOffset = 256, kPowSeqOffset = 320;  // mapped mailbox bytes
+
+struct PowPost {
+    unsigned int *ticket;
+    unsigned long long *best;  // device view of mapped host memory
+    uint32_t *seq;             // device view of mapped host memory
+    uint32_t seq_val;
+};
 
 struct PowBlock {
     uint32_t w[16];  // prefix words, zero where the nonce goes
@@ -53,13 +64,16 @@ __device__ __forceinline__ bool pow_pass(const uint32_t h[8], uint32_t bits) {
 __global__ void __launch_bounds__(kPowThreads) pow_scan_kernel(PowBlock blk, uint32_t block_len,
                                                                uint32_t nonce_off, uint32_t bits,
                                                                uint64_t start, uint64_t span,
-                                                               unsigned long long *ctl) {
+                                                               uint32_t per,
+                                                               unsigned long long *ctl,
+                                                               PowPost post) {
     __shared__ unsigned long long s_base;
     __shared__ int s_stop;
     const uint32_t wi = nonce_off >> 2, sh = (nonce_off & 3) * 8;
+    const unsigned long long chunk = (unsigned long long)kPowThreads * per;
     for (;;) {
         if (threadIdx.x == 0) {
-            const unsigned long long base = atomicAdd(&ctl[0], (unsigned long long)kPowChunk);
+            const unsigned long long base = atomicAdd(&ctl[0], chunk);
             const unsigned long long best = *(volatile unsigned long long *)&ctl[1];
             s_base = base;
             s_stop = base >= span || start + base > best;
@@ -68,9 +82,9 @@ __global__ void __launch_bounds__(kPowThreads) pow_scan_kernel(PowBlock blk, uin
         const uint64_t base = s_base;
         const int stop = s_stop;
         __syncthreads();
-        if (stop) return;
+        if (stop) break;
 #pragma unroll 1
-        for (int i = 0; i < kPowPerThread; ++i) {
+        for (uint32_t i = 0; i < per; ++i) {
             const uint64_t rel = base + (uint64_t)i * kPowThreads + threadIdx.x;
             if (rel >= span) break;
             const uint64_t nonce = start + rel;
@@ -90,6 +104,20 @@ __global__ void __launch_bounds__(kPowThreads) pow_scan_kernel(PowBlock blk, uin
             bz::b3_compress_cv(h, m, 0, block_len,
                                bz::B3_CHUNK_START | bz::B3_CHUNK_END | bz::B3_ROOT);
             if (pow_pass(h, bits)) atomicMin(&ctl[1], (unsigned long long)nonce);
+        }
+    }
+    // every hit of this block was recorded before the barrier that preceded
+    // the stop; the last block to leave posts the minimum and resets
+    if (threadIdx.x == 0) {
+        __threadfence();
+        if (atomicAdd(post.ticket, 1u) == gridDim.x - 1) {
+            __threadfence();
+            *(volatile unsigned long long *)post.best = *(volatile unsigned long long *)&ctl[1];
+            asm volatile("st.release.sys.global.u32 [%0], %1;" ::"l"(post.seq), "r"(post.seq_val)
+                         : "memory");
+            ctl[0] = 0;
+            ctl[1] = ~0ull;
+            *post.ticket = 0;
         }
     }
 }
@@ -116,25 +144,46 @@ int bz_pow_first_nonce(bz_ctx *ctx, const uint8_t *prefix, size_t prefix_len, ui
                    ((uint32_t)bytes[4 * i + 2] << 16) | ((uint32_t)bytes[4 * i + 3] << 24);
     unsigned long long *ctl =
         (unsigned long long *)((uint8_t *)ctx->d_small + kPowCtlOffset);
-    const unsigned long long *h_best =
-        (const unsigned long long *)((uint8_t *)ctx->h_small + kPowCtlOffset);
-    // enough blocks for ~4 expected hits' worth of nonces, at most 8 per SM
-    const double want = ldexp(4.0, bits < 60 ? (int)bits : 60) / (double)kPowChunk;
-    const int max_blocks = ctx->num_sms * 8;
-    const int blocks = want >= max_blocks ? max_blocks : (want < 1.0 ? 1 : (int)want);
-    for (uint64_t s = start; s < end;) {
-        const uint64_t span = end - s < kPowWindow ? end - s : kPowWindow;
+    unsigned int *ticket = (unsigned int *)(ctl + 2);
+    if (!ctx->pow_ready) {
         BZ_CUDA(ctx, cudaMemsetAsync(ctl, 0, 8, ctx->stream));
         BZ_CUDA(ctx, cudaMemsetAsync(ctl + 1, 0xFF, 8, ctx->stream));
+        BZ_CUDA(ctx, cudaMemsetAsync(ticket, 0, 4, ctx->stream));
+        ctx->pow_ready = true;
+    }
+    // one nonce per thread per chunk for short searches (the first chunks end
+    // sooner), four above 20 bits; enough blocks for ~4 expected hits' worth
+    // of nonces, at most 8 per SM
+    const uint32_t per = bits <= 20 ? 1u : (uint32_t)kPowPerThread;
+    const double chunk = (double)kPowThreads * per;
+    const double want = ldexp(4.0, bits < 60 ? (int)bits : 60) / chunk;
+    const int max_blocks = ctx->num_sms * 8;
+    const int blocks = want >= max_blocks ? max_blocks : (want < 1.0 ? 1 : (int)want);
+    PowPost post;
+    post.ticket = ticket;
+    post.best = (unsigned long long *)((uint8_t *)ctx->d_mbox + kPowBestOffset);
+    post.seq = (uint32_t *)((uint8_t *)ctx->d_mbox + kPowSeqOffset);
+    for (uint64_t s = start; s < end;) {
+        const uint64_t span = end - s < kPowWindow ? end - s : kPowWindow;
+        if (++ctx->pow_seq == 0) ++ctx->pow_seq;
+        post.seq_val = ctx->pow_seq;
         pow_scan_kernel<<<blocks, kPowThreads, 0, ctx->stream>>>(
-            blk, (uint32_t)(prefix_len + 8), (uint32_t)prefix_len, bits, s, span, ctl);
+            blk, (uint32_t)(prefix_len + 8), (uint32_t)prefix_len, bits, s, span, per, ctl, post);
         ctx->launches += 1;
-        BZ_CUDA(ctx, cudaGetLastError());
-        BZ_CUDA(ctx, cudaMemcpyAsync((void *)h_best, ctl + 1, 8, cudaMemcpyDeviceToHost,
-                                     ctx->stream));
-        BZ_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
-        if (*h_best != ~0ull) {
-            *nonce = *h_best;
+        const cudaError_t e = cudaGetLastError();
+        if (e != cudaSuccess) {
+            ctx->pow_ready = false;
+            return bz::set_err(ctx, BZ_ERR_CUDA, "pow_scan_kernel launch", e);
+        }
+        const int rc = bz::mapped_wait(ctx, kPowSeqOffset, post.seq_val, "proof-of-work search");
+        if (rc) {
+            ctx->pow_ready = false;
+            return rc;
+        }
+        const unsigned long long best =
+            *(const volatile unsigned long long *)((uint8_t *)ctx->h_mbox + kPowBestOffset);
+        if (best != ~0ull) {
+            *nonce = best;
             return BZ_OK;
         }
         s += span;

@@ -852,21 +852,26 @@ void reset_msg_ticket(bz_ctx *ctx) {
 // {u0, u2}.  The wait spins on the mailbox (no stream synchronisation on the
 // critical path), checking the stream every few hundred spins so that a
 // failed launch returns its error, and gives up after 60 s.
-int msg_wait(bz_ctx *ctx, uint32_t seq, uint64_t u0[2], uint64_t u2[2]) {
-    volatile uint32_t *sp = (volatile uint32_t *)((uint8_t *)ctx->h_mbox + 64);
+int mapped_wait(bz_ctx *ctx, size_t offset, uint32_t seq, const char *what) {
+    volatile uint32_t *sp = (volatile uint32_t *)((uint8_t *)ctx->h_mbox + offset);
     const auto t0 = std::chrono::steady_clock::now();
     for (uint64_t spin = 1; *sp != seq; ++spin) {
         if ((spin & 255) == 0) {
             const cudaError_t e = cudaStreamQuery(ctx->stream);
-            if (e != cudaSuccess && e != cudaErrorNotReady)
-                return set_err(ctx, BZ_ERR_CUDA, "sumcheck message kernel", e);
+            if (e != cudaSuccess && e != cudaErrorNotReady) return set_err(ctx, BZ_ERR_CUDA, what, e);
             if (e == cudaSuccess && *sp != seq)
-                return set_msg(ctx, BZ_ERR_CUDA, "sumcheck message not posted");
+                return set_msg(ctx, BZ_ERR_CUDA, std::string(what) + ": result not posted");
             if (std::chrono::steady_clock::now() - t0 > std::chrono::seconds(60))
-                return set_msg(ctx, BZ_ERR_TIMEOUT, "sumcheck message wait");
+                return set_msg(ctx, BZ_ERR_TIMEOUT, std::string(what) + ": wait");
         }
     }
     std::atomic_thread_fence(std::memory_order_acquire);
+    return BZ_OK;
+}
+
+int msg_wait(bz_ctx *ctx, uint32_t seq, uint64_t u0[2], uint64_t u2[2]) {
+    const int rc = mapped_wait(ctx, 64, seq, "sumcheck message");
+    if (rc) return rc;
     const volatile uint64_t *h = (const volatile uint64_t *)ctx->h_mbox;
     if (u0) {
         u0[0] = h[0];

@@ -57,6 +57,8 @@ struct bz_ctx {
     uint32_t mbox_seq = 0;    // last posted sequence number
     uint32_t gate_seq = 0;    // last armed fold's gate number
     bool arm_folds = true;    // cleared after a gate ran out (the prover stops arming)
+    uint32_t pow_seq = 0;     // last proof-of-work search's mailbox number
+    bool pow_ready = false;   // the search's device counters hold their idle values
     cudaEvent_t ev0 = nullptr, ev1 = nullptr;
     std::mutex aux_mu;
     std::map<cudaStream_t, bz_aux_stream> aux;
@@ -141,6 +143,10 @@ int fold_cancel(bz_ctx *ctx, ArmedFold *a);
 // context.
 bool gate_gave_up(bz_ctx *ctx);
 int msg_wait(bz_ctx *ctx, uint32_t seq, uint64_t u0[2], uint64_t u2[2]);
+// Spin until the 32-bit word at byte `offset` of the mapped mailbox reads
+// seq, checking the context stream for errors (and for having gone idle
+// without posting) every few hundred spins; 60 s limit.
+int mapped_wait(bz_ctx *ctx, size_t offset, uint32_t seq, const char *what);
 // Zero the message ticket (after a round that may have stopped part-way).
 void reset_msg_ticket(bz_ctx *ctx);
 }  // namespace bz
