@@ -612,6 +612,48 @@ __global__ void ntt_generic_layer(const uint4 *src, uint4 *dst, const uint4 *tw,
     }
 }
 
+// The whole transform of a small shape in one launch: one CTA per lane holds
+// the lane's 2^ell codeword positions in shared memory (the replicated
+// message, read through the position mask as the first table pass does), and
+// each thread does one butterfly per layer with the generic multiply.  The
+// layers, blocks and twiddles are those of ntt_generic_layer.
+__global__ void __launch_bounds__(512) ntt_small_kernel(const uint4 *msg, uint4 *cw,
+                                                        const uint4 *tw, int ell, int r,
+                                                        int log_lanes, int msg_pos_bits) {
+    extern __shared__ uint4 col[];
+    const uint32_t P = 1u << ell;
+    const uint64_t lane = blockIdx.x;
+    const uint32_t msg_mask = (1u << msg_pos_bits) - 1;
+    for (uint32_t p = threadIdx.x; p < P; p += blockDim.x)
+        col[p] = msg[((uint64_t)(p & msg_mask) << log_lanes) | lane];
+    for (int layer = r; layer < ell; ++layer) {
+        __syncthreads();
+        const int log_h = ell - layer - 1;
+        for (uint32_t pair = threadIdx.x; pair < P / 2; pair += blockDim.x) {
+            const uint32_t B = pair >> log_h, rr = pair & ((1u << log_h) - 1);
+            const uint32_t p0 = (B << (log_h + 1)) + rr, p1 = p0 + (1u << log_h);
+            const uint4 t = tw[(1u << layer) + B];
+            uint4 u = col[p0], w = col[p1];
+            u = gf_add(u, gf_mul(w, t));
+            w = gf_add(w, u);
+            col[p0] = u;
+            col[p1] = w;
+        }
+    }
+    __syncthreads();
+    for (uint32_t p = threadIdx.x; p < P; p += blockDim.x)
+        cw[((uint64_t)p << log_lanes) | lane] = col[p];
+}
+
+// Shapes small enough for ntt_small_kernel to beat the table passes (the
+// recursive levels' commits and small requests).  Measured on GB300: 2^12
+// elements as 64 lanes of 2^8 positions 11.9 us against 30.4 us for the pass
+// sequence, 2^14 as 128 lanes of 2^9 positions 15.7 against 33.3 us; at 256
+// lanes of 2^10 positions (2^16 elements) the passes win, 31 against 42 us.
+static bool small_ntt_ok(const Shape &s) {
+    return s.log_dim() >= 1 && s.k_code() <= 9 && s.log_lanes <= 8;
+}
+
 // cw[rep * N + i] = msg[i] for every replica (commit.rs:239-258).
 __global__ void replicate_fill(const uint4 *msg, uint4 *cw, uint64_t msg_words, int reps) {
     for (uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; i < msg_words;
@@ -784,6 +826,13 @@ int launch_ntt(const Shape &s, uint32_t schedule, const uint4 *d_msg, uint4 *d_c
         return 1;
     }
     const bool generic = (schedule & SCHED_GENERIC) != 0;
+    if (!generic && small_ntt_ok(s)) {
+        const unsigned threads = (unsigned)std::min<uint64_t>(P / 2, 512);
+        ntt_small_kernel<<<1u << L, threads, P * sizeof(uint4), st>>>(d_msg, d_cw, d_tw, ell, r,
+                                                                      L, b);
+        mark("ntt_small");
+        return 1;
+    }
     if (generic) {
         for (int layer = r; layer < ell; ++layer) {
             const uint64_t n_tasks = ((uint64_t)1 << (ell - 1)) << L;
