@@ -612,17 +612,20 @@ def _bench_open(ctx, bz, msg, params):
     cfg = bz.LigeritoConfig(**open_config(params.log_batch_size))
 
     def timed(fn, reps=OPEN_REPS + 1):
-        ts, out = [], None
+        # the previous rep's result is released outside the timed region
+        ts, out, last = [], None, None
         for _ in range(reps):
             t = bz.Blake3Transcript()
             t.absorb_slice(b"bench opening")
+            last = None
             ctx.synchronize()
             t0 = time.perf_counter()
             out = fn(t)
             ts.append(time.perf_counter() - t0)
             if hasattr(out, "free"):
                 out.free()
-        return statistics.median(ts[1:]) * 1e3, min(ts[1:]) * 1e3, out
+            last, out = out, None
+        return statistics.median(ts[1:]) * 1e3, min(ts[1:]) * 1e3, last
 
     prove_ms, prove_min, proof = timed(lambda t: bz.prove(t, pd, msg, b, [1, 2], cfg, ctx))
     prove_c_ms, _, _ = timed(lambda t: bz.prove(t, pd, msg, b, [1, 2], cfg, ctx, decode=False))
@@ -685,6 +688,7 @@ def _bench_bit_mle(ctx, bz):
         op.write(w)
         nbytes = len(w.into_bytes())
         pd.free()
+        del op, r0, w, t, c  # released here, not inside the next rep's timed calls
         for k, v in zip(ts, (t1 - t0, t2 - t1, t3 - t2)):
             ts[k].append(v * 1e3)
     d.free()

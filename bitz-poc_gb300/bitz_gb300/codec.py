@@ -54,7 +54,8 @@ def _hs(a) -> np.ndarray:
 
 @dataclass
 class RecursiveProof:
-    opened_rows: list = field(default_factory=list)     # list of (len, 2) uint64 arrays
+    # (len, 2) uint64 arrays: a list, or one (rows, len, 2) array when decoded
+    opened_rows: list = field(default_factory=list)
     merkle_proof: np.ndarray = field(default_factory=lambda: np.zeros((0, 32), np.uint8))
 
 
@@ -92,6 +93,10 @@ class _Keep:
 
 
 def _rows_view(keep: _Keep, rows) -> RowsView:
+    if isinstance(rows, np.ndarray) and rows.ndim == 3:
+        data = np.ascontiguousarray(rows, dtype=np.uint64).reshape(-1, 2)
+        lens = np.full(rows.shape[0], rows.shape[1], dtype=np.uintp)
+        return RowsView(rows.shape[0], keep.arr(lens, _S), keep.arr(data, ctypes.c_uint64))
     rows = [_gfs(r) for r in rows]
     lens = np.array([r.shape[0] for r in rows], dtype=np.uintp)
     data = np.concatenate(rows) if rows else np.zeros((0, 2), np.uint64)
@@ -146,9 +151,11 @@ class _ProofOwner:
             self.h = None
 
 
-def _rows_from(rv: RowsView, owner: _ProofOwner | None = None) -> list:
-    """Opened rows as (lanes, 2) arrays: views into the native proof when an
-    owner keeps it alive (no copy of the rows), copies otherwise."""
+def _rows_from(rv: RowsView, owner: _ProofOwner | None = None):
+    """Opened rows, each a (lanes, 2) array: views into the native proof when
+    an owner keeps it alive (no copy of the rows), copies otherwise.  Rows of
+    one length (every opening's) come as a single (rows, lanes, 2) array,
+    which indexes and iterates row by row like the list it stands for."""
     if not rv.n_rows:
         return []
     lens = np.ctypeslib.as_array(rv.row_lens, shape=(rv.n_rows,)).astype(np.int64)
@@ -162,6 +169,8 @@ def _rows_from(rv: RowsView, owner: _ProofOwner | None = None) -> list:
             ctypes.cast(rv.data, ctypes.c_void_p).value)
         buf._owner = owner
         flat = np.frombuffer(buf, dtype=np.uint64)
+    if (lens == lens[0]).all():
+        return flat.reshape(rv.n_rows, int(lens[0]), 2)
     return np.split(flat.reshape(total, 2), np.cumsum(lens)[:-1])
 
 
