@@ -146,7 +146,8 @@ int launch_round_msg(const uint4 *d_f, const uint4 *d_b, size_t n, uint64_t *d_p
                      const MsgPost *post = nullptr);
 int launch_partial_eval_round(const uint4 *d_in, size_t n, uint4 r, uint4 *d_out,
                               cudaStream_t st);
-int launch_build_eq(const uint4 *d_point_dev, size_t k, uint4 *d_out, cudaStream_t st);
+int launch_build_eq(const uint4 *d_point_dev, size_t k, uint4 *d_out, cudaStream_t st,
+                    int num_sms);
 int launch_sv_fold(const uint4 *d_packed, const uint4 *d_eq, size_t n, uint64_t *d_partials,
                    uint4 *d_sv, cudaStream_t st, int num_sms);
 size_t sv_partials_bytes(size_t n, int num_sms);

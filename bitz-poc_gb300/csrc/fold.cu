@@ -368,9 +368,61 @@ __global__ void __launch_bounds__(512) eq_small_kernel(uint4 *eq, const uint4 *p
     }
 }
 
+// eq over k variables in one launch, as the product of two half tables:
+// eq[j] = lo[j mod 2^a] * hi[j >> a], lo over point[0..a) and hi over
+// point[a..k).  Every factor of an entry is the same field element as in the
+// doubling rounds (bit i of j picks r_i or 1 + r_i), so the entries are
+// identical.  Each CTA builds both halves in shared memory (their rounds side
+// by side), then writes its share of the products.
+constexpr int kEqSplitMaxK = 22;
+__global__ void __launch_bounds__(512) eq_split_kernel(uint4 *eq, const uint4 *point, int k,
+                                                       int a) {
+    extern __shared__ uint4 halves[];
+    const int b = k - a;
+    uint4 *lo = halves, *hi = halves + ((size_t)1 << a);
+    if (threadIdx.x == 0) {
+        lo[0] = make_uint4(1, 0, 0, 0);
+        hi[0] = make_uint4(1, 0, 0, 0);
+    }
+    __syncthreads();
+    for (int i = 0; i < (a > b ? a : b); ++i) {
+        const uint32_t nlo = i < a ? 1u << i : 0u, nhi = i < b ? 1u << i : 0u;
+        for (uint32_t j = threadIdx.x; j < nlo + nhi; j += blockDim.x) {
+            const bool in_lo = j < nlo;
+            uint4 *t = in_lo ? lo : hi;
+            const uint32_t jj = in_lo ? j : j - nlo;
+            const uint4 r = point[in_lo ? i : a + i];
+            const uint4 p = t[jj];
+            const uint4 one = gf_mul(p, r);
+            t[(1u << i) + jj] = one;
+            t[jj] = gf_add(p, one);
+        }
+        __syncthreads();
+    }
+    const uint64_t n = (uint64_t)1 << k;
+    const uint64_t mask = ((uint64_t)1 << a) - 1;
+    for (uint64_t j = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; j < n;
+         j += (uint64_t)gridDim.x * blockDim.x)
+        eq[j] = gf_mul(lo[j & mask], hi[j >> a]);
+}
+
 constexpr size_t kEqSmallRounds = 12;
 
-int launch_build_eq(const uint4 *d_point, size_t k, uint4 *d_out, cudaStream_t st) {
+// Up to 6 variables: the doubling rounds in one CTA.  Up to 22: one split
+// launch (2^12 entries: 3 to 4 us of products after 6 half-table rounds,
+// against 12 rounds in one CTA; 2^20: one launch instead of nine).  Above:
+// 12 rounds in one CTA, then one launch per further round.
+int launch_build_eq(const uint4 *d_point, size_t k, uint4 *d_out, cudaStream_t st,
+                    int num_sms) {
+    if (k > 6 && k <= (size_t)kEqSplitMaxK) {
+        const int a = (int)k / 2;
+        const size_t smem = (((size_t)1 << a) + ((size_t)1 << (k - a))) * sizeof(uint4);
+        const uint64_t n = (uint64_t)1 << k;
+        const unsigned grid = (unsigned)std::max<uint64_t>(
+            1, std::min<uint64_t>((n + 511) / 512, (uint64_t)2 * num_sms));
+        eq_split_kernel<<<grid, 512, smem, st>>>(d_out, d_point, (int)k, a);
+        return 1;
+    }
     const size_t k0 = std::min(k, kEqSmallRounds);
     eq_small_kernel<<<1, 512, 0, st>>>(d_out, d_point, (int)k0);
     for (size_t i = k0; i < k; ++i) {
@@ -478,6 +530,8 @@ __global__ void __launch_bounds__(256) phi_kernel(const uint4 *eq_hi, uint64_t n
 
 void init_fold_kernels() {
     cudaFuncSetAttribute(phi_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, 65536);
+    cudaFuncSetAttribute(eq_split_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                         (int)((2u << (kEqSplitMaxK / 2)) * sizeof(uint4)));
     cudaFuncSetAttribute(fold_and_msg_kernel<false>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                          (int)kRTableSmem);
     cudaFuncSetAttribute(fold_and_msg_kernel<true>, cudaFuncAttributeMaxDynamicSharedMemorySize,

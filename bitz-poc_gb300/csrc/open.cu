@@ -213,7 +213,7 @@ struct Sumcheck {
             for (uint32_t i = 0; i < n; ++i) tr->sample_f128(&z[2 * i]);
             if (n) cudaMemcpyAsync(d_z, z.data(), 16 * (size_t)n, cudaMemcpyHostToDevice,
                                    ctx->stream);
-            ctx->launches += bz::launch_build_eq(d_z, n, d_eq, ctx->stream);
+            ctx->launches += bz::launch_build_eq(d_z, n, d_eq, ctx->stream, ctx->num_sms);
             uint64_t u0[2], u2[2], y[2];
             rc = bz_round_msg_lsb(ctx, f, (const uint64_t *)d_eq, len, u0, u2);
             if (rc) break;
@@ -326,7 +326,7 @@ int induce_basis(bz_ctx *ctx, uint32_t log_msg_cols, uint32_t rate,
     if (n_alpha)
         cudaMemcpyAsync(d_alpha, alpha.data(), 16 * n_alpha, cudaMemcpyHostToDevice, ctx->stream);
     if (q) cudaMemcpyAsync(d_pos, queries.data(), 8 * q, cudaMemcpyHostToDevice, ctx->stream);
-    ctx->launches += bz::launch_build_eq(d_alpha, n_alpha, d_w, ctx->stream);
+    ctx->launches += bz::launch_build_eq(d_alpha, n_alpha, d_w, ctx->stream, ctx->num_sms);
     ctx->launches += bz::launch_induce_basis(d_dom, log_d, d_pos, d_w, (int)q, d_tw, ctx->stream);
     if (cudaGetLastError() != cudaSuccess) {
         bz::dev_free(ctx, mem, bytes, false);

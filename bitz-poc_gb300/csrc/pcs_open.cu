@@ -109,8 +109,8 @@ struct EqSplit {
         if (vars)
             cudaMemcpyAsync(d_pt, point.data(), 16 * (size_t)vars, cudaMemcpyHostToDevice,
                             ctx->stream);
-        ctx->launches += bz::launch_build_eq(d_pt, (size_t)lo, tail, ctx->stream);
-        ctx->launches += bz::launch_build_eq(d_pt + lo, hi_vars, head, ctx->stream);
+        ctx->launches += bz::launch_build_eq(d_pt, (size_t)lo, tail, ctx->stream, ctx->num_sms);
+        ctx->launches += bz::launch_build_eq(d_pt + lo, hi_vars, head, ctx->stream, ctx->num_sms);
         return cudaGetLastError() == cudaSuccess ? BZ_OK
                                                  : bz::set_msg(ctx, BZ_ERR_CUDA, "eq tables");
     }

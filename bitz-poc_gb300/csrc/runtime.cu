@@ -1060,7 +1060,8 @@ int bz_build_eq_lsb(bz_ctx *ctx, const uint64_t *point, size_t k, uint64_t *d_ou
     int rc = dev_alloc(ctx, (k ? k : 1) * 16, &d_pt, false);
     if (rc) return rc;
     if (k) cudaMemcpyAsync(d_pt, point, k * 16, cudaMemcpyHostToDevice, ctx->stream);
-    ctx->launches += launch_build_eq((const uint4 *)d_pt, k, (uint4 *)d_out, ctx->stream);
+    ctx->launches +=
+        launch_build_eq((const uint4 *)d_pt, k, (uint4 *)d_out, ctx->stream, ctx->num_sms);
     dev_free(ctx, d_pt, 0, false);
     BZ_CUDA(ctx, cudaGetLastError());
     BZ_CUDA(ctx, cudaStreamSynchronize(ctx->stream));

@@ -113,6 +113,16 @@ def test_partial_eval(oracle, ctx, n, k):
     assert (out.to_host() == oracle.partial_eval_lsb(f, rs)).all()
 
 
+@pytest.mark.parametrize("k", [0, 1, 6, 7, 12, 13, 20, 22, 23])
+def test_build_eq(oracle, ctx, k):
+    """eq tables: doubling rounds (k <= 6, k > 22) and the split launch
+    (lo x hi half tables) give the oracle's entries."""
+    from bitz_gb300.ligerito import build_eq_lsb
+
+    pt = _rand(np.random.default_rng(300 + k), k)
+    assert (build_eq_lsb(pt, ctx).to_host() == oracle.build_eq_lsb(pt)).all()
+
+
 @pytest.mark.parametrize("k", [1, 5, 12])
 def test_ring_switch_passes(oracle, ctx, k):
     from bitz_gb300 import DeviceArray
