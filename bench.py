@@ -717,7 +717,7 @@ def _bench_serve(ctx, bz, args, plain_rate=None):
     saturating point (1.5 x) serves ``--serve-requests`` requests (10k by
     default); the lighter loads a tenth of that.  Each request is one
     ``submit_commit_open`` (the server queues the opening when the commit
-    completes) and the driver reacts to the server's completion queue."""
+    completes) and the request loop reacts to the server's completion queue."""
     import numpy as np
     from bitz_gb300 import serve as S
 
