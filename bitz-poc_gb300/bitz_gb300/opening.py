@@ -76,8 +76,9 @@ class L0Opening:
         gn = ctypes.c_uint64()
         qs = np.zeros(max(sz.n_queries, 1), np.uint64)
         al = np.zeros((max(sz.n_alpha, 1), 2), np.uint64)
-        rows = np.zeros((max(sz.n_queries, 1), sz.row_len, 2), np.uint64)
-        proof = np.zeros((max(sz.n_proof_hashes, 1), 32), np.uint8)
+        # filled by the copy below: no zeroing, and the rows are kept as copied
+        rows = np.empty((max(sz.n_queries, 1), sz.row_len, 2), np.uint64)
+        proof = np.empty((max(sz.n_proof_hashes, 1), 32), np.uint8)
         check(ctx.handle, lib().bz_l0_opening_copy(handle, ptr(sc), ptr(fn), ptr(ch), root1,
                                                    ctypes.byref(gn), ptr(qs), ptr(al), ptr(rows),
                                                    ptr(proof)))
@@ -88,8 +89,8 @@ class L0Opening:
         self.grinding_nonce = int(gn.value)
         self.queries = [int(x) for x in qs[:sz.n_queries]]
         self.alpha = al[:sz.n_alpha].copy()
-        self.opened_rows = rows[:sz.n_queries].copy()
-        self.merkle_proof = proof[:sz.n_proof_hashes].copy()
+        self.opened_rows = rows[:sz.n_queries]
+        self.merkle_proof = proof[:sz.n_proof_hashes]
         ov = np.zeros((max(sz.n_ood_values, 1), 2), np.uint64)
         check(ctx.handle, lib().bz_l0_opening_ood_values(handle, ptr(ov)))
         self.ood_values = ov[:sz.n_ood_values].copy()
