@@ -152,7 +152,7 @@ int launch_sv_fold(const uint4 *d_packed, const uint4 *d_eq, size_t n, uint64_t 
                    uint4 *d_sv, cudaStream_t st, int num_sms);
 size_t sv_partials_bytes(size_t n, int num_sms);
 int launch_phi(const uint4 *d_eq_hi, size_t n, const uint4 *d_eq_r2, uint4 *d_out,
-               cudaStream_t st);
+               cudaStream_t st, int num_sms);
 
 int launch_chacha(uint64_t seed, uint64_t first_word, uint4 *d_out, size_t n_words,
                   cudaStream_t st);

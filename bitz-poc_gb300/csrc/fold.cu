@@ -540,10 +540,12 @@ void init_fold_kernels() {
                          (int)kRTableSmem);
 }
 
+// Two CTAs per SM at most: every CTA builds the 64 KB of tables first, so a
+// grid-stride loop over fewer CTAs builds them fewer times.
 int launch_phi(const uint4 *d_eq_hi, size_t n, const uint4 *d_eq_r2, uint4 *d_out,
-               cudaStream_t st) {
+               cudaStream_t st, int num_sms) {
     const unsigned grid = (unsigned)std::max<uint64_t>(
-        1, std::min<uint64_t>((n + 255) / 256, 2048));
+        1, std::min<uint64_t>((n + 255) / 256, (uint64_t)2 * num_sms));
     phi_kernel<<<grid, 256, 65536, st>>>(d_eq_hi, n, d_eq_r2, d_out);
     return 1;
 }

@@ -154,12 +154,27 @@ __global__ void __launch_bounds__(kThreads) split_dot_kernel(const uint4 *p, con
 }
 
 // b[i] += (eta * head[i >> lo]) * tail[i & (2^lo - 1)]  (add_ood_basis,
-// src/ligerito_flock.rs:1590-1650: eta * eq(point) added to the basis)
-__global__ void eq_axpy_kernel(uint4 *b, const uint4 *tail, int lo, const uint4 *head, uint4 eta,
-                               uint64_t n) {
+// src/ligerito_flock.rs:1590-1650: eta * eq(point) added to the basis).  When
+// a CTA's elements share one head entry (2^lo >= the CTA size), its thread 0
+// forms eta * head once for all of them.
+constexpr int kLogThreads = 8;
+static_assert((1 << kLogThreads) == kThreads, "eq_axpy assumes 256-thread CTAs");
+__global__ void __launch_bounds__(kThreads) eq_axpy_kernel(uint4 *b, const uint4 *tail, int lo,
+                                                           const uint4 *head, uint4 eta,
+                                                           uint64_t n) {
     const uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    uint4 s;
+    if (lo >= kLogThreads) {
+        __shared__ uint4 s_cta;
+        if (threadIdx.x == 0)
+            s_cta = gf_mul(eta, head[((uint64_t)blockIdx.x * blockDim.x) >> lo]);
+        __syncthreads();
+        s = s_cta;
+    } else {
+        if (i >= n) return;
+        s = gf_mul(eta, head[i >> lo]);
+    }
     if (i >= n) return;
-    const uint4 s = gf_mul(eta, head[i >> lo]);
     b[i] = gf_add(b[i], gf_mul(s, tail[i & (((uint64_t)1 << lo) - 1)]));
 }
 

@@ -1090,7 +1090,7 @@ int bz_phi_from_words(bz_ctx *ctx, const uint64_t *d_eq_hi, size_t n, const uint
     if (rc) return rc;
     cudaMemcpyAsync(d_r2, eq_r2, 128 * 16, cudaMemcpyHostToDevice, ctx->stream);
     ctx->launches += launch_phi((const uint4 *)d_eq_hi, n, (const uint4 *)d_r2, (uint4 *)d_out,
-                                ctx->stream);
+                                ctx->stream, ctx->num_sms);
     dev_free(ctx, d_r2, 0, false);
     BZ_CUDA(ctx, cudaGetLastError());
     BZ_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
