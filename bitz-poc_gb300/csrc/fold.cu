@@ -434,12 +434,16 @@ int launch_build_eq(const uint4 *d_point, size_t k, uint4 *d_out, cudaStream_t s
 }
 
 // sv[j] = sum_y eq[y] * bit_j(P[y]) (src/ligerito.rs:317-375).  128 threads
-// per CTA, one per output bit j; the CTA stages a tile of (P, eq) in shared
-// memory and every thread scans it (broadcast reads).
+// per CTA, one per output bit j.  For each tile of 256 y the CTA stages P in
+// shared memory and, per group of 4 consecutive y, the 16 XORs of eq over
+// every subset of the group.  Thread j gathers bit j of the group's 4 P words
+// into a 4-bit index and adds that subset's sum: one lookup per 4 y instead
+// of 4 masked additions.
 constexpr int kSvTile = 256;
 __global__ void __launch_bounds__(128) sv_fold_kernel(const uint4 *packed, const uint4 *eq,
                                                       uint64_t n, uint4 *partials) {
-    __shared__ uint4 sp[kSvTile], se[kSvTile];
+    __shared__ uint32_t sp[kSvTile][4];
+    __shared__ uint4 sub[kSvTile / 4][16];
     const int j = threadIdx.x;
     const int wsel = j >> 5;
     const uint32_t bit = j & 31;
@@ -449,20 +453,38 @@ __global__ void __launch_bounds__(128) sv_fold_kernel(const uint4 *packed, const
         __syncthreads();
         for (int i = threadIdx.x; i < kSvTile; i += blockDim.x) {
             const uint64_t y = base + i;
-            sp[i] = y < n ? packed[y] : make_uint4(0, 0, 0, 0);
-            se[i] = y < n ? eq[y] : make_uint4(0, 0, 0, 0);
+            const uint4 v = y < n ? packed[y] : make_uint4(0, 0, 0, 0);
+            sp[i][0] = v.x;
+            sp[i][1] = v.y;
+            sp[i][2] = v.z;
+            sp[i][3] = v.w;
+        }
+        {
+            // thread t builds subsets 8h .. 8h+7 of group g = t / 2 (h = t mod 2)
+            const int g = threadIdx.x >> 1, h = threadIdx.x & 1;
+            uint4 e[4];
+#pragma unroll
+            for (int k = 0; k < 4; ++k) {
+                const uint64_t y = base + 4 * g + k;
+                e[k] = y < n ? eq[y] : make_uint4(0, 0, 0, 0);
+            }
+#pragma unroll
+            for (int q = 0; q < 8; ++q) {
+                const int m = 8 * h + q;
+                uint4 t = make_uint4(0, 0, 0, 0);
+#pragma unroll
+                for (int k = 0; k < 4; ++k)
+                    if ((m >> k) & 1) t = gf_add(t, e[k]);
+                sub[g][m] = t;
+            }
         }
         __syncthreads();
-#pragma unroll 8
-        for (int i = 0; i < kSvTile; ++i) {
-            const uint4 p = sp[i];
-            const uint32_t w = wsel == 0 ? p.x : wsel == 1 ? p.y : wsel == 2 ? p.z : p.w;
-            const uint32_t m = 0u - ((w >> bit) & 1u);
-            const uint4 e = se[i];
-            acc.x ^= e.x & m;
-            acc.y ^= e.y & m;
-            acc.z ^= e.z & m;
-            acc.w ^= e.w & m;
+#pragma unroll 4
+        for (int g = 0; g < kSvTile / 4; ++g) {
+            uint32_t idx = 0;
+#pragma unroll
+            for (int k = 0; k < 4; ++k) idx |= ((sp[4 * g + k][wsel] >> bit) & 1u) << k;
+            acc = gf_add(acc, sub[g][idx]);
         }
     }
     partials[(uint64_t)blockIdx.x * 128 + j] = acc;
