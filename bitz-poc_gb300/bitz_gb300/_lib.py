@@ -95,6 +95,8 @@ _SIGS = {
     "bz_ligerito_open_l0": (_I, [_P, _P, _P, _P, _P, _P, _P, _PP]),
     "bz_l0_opening_sizes": (_I, [_P, _P]),
     "bz_l0_opening_copy": (_I, [_P, _P, _P, _P, _P, _P, _P, _P, _P, _P]),
+    "bz_l0_opening_take_rows": (_I, [_P, _PP, ctypes.POINTER(ctypes.POINTER(ctypes.c_uint64))]),
+    "bz_rows_free": (_I, [_P]),
     "bz_l0_opening_level1": (_P, [_P]),
     "bz_l0_opening_folded": (_I, [_P, _PP, _PP, ctypes.POINTER(_S)]),
     "bz_l0_opening_free": (_I, [_P]),

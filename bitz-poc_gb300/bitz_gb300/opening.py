@@ -57,6 +57,19 @@ class L0Config:
                          self.hash_kind, self.ood_samples1)
 
 
+class _RowsOwner:
+    """Owns opened rows moved out of a native level-0 opening; freed when the
+    last array viewing them is gone."""
+
+    def __init__(self, h):
+        self.h = h
+
+    def __del__(self):
+        if getattr(self, "h", None):
+            lib().bz_rows_free(self.h)
+            self.h = None
+
+
 class L0Opening:
     """Results of one level-0 opening; owns the level-1 commitment and the
     folded arrays on the device until ``free``."""
@@ -76,12 +89,24 @@ class L0Opening:
         gn = ctypes.c_uint64()
         qs = np.zeros(max(sz.n_queries, 1), np.uint64)
         al = np.zeros((max(sz.n_alpha, 1), 2), np.uint64)
-        # filled by the copy below: no zeroing, and the rows are kept as copied
-        rows = np.empty((max(sz.n_queries, 1), sz.row_len, 2), np.uint64)
         proof = np.empty((max(sz.n_proof_hashes, 1), 32), np.uint8)
         check(ctx.handle, lib().bz_l0_opening_copy(handle, ptr(sc), ptr(fn), ptr(ch), root1,
-                                                   ctypes.byref(gn), ptr(qs), ptr(al), ptr(rows),
+                                                   ctypes.byref(gn), ptr(qs), ptr(al), None,
                                                    ptr(proof)))
+        # the opened rows move out of the opening and are viewed in place
+        rh = ctypes.c_void_p()
+        data = ctypes.POINTER(ctypes.c_uint64)()
+        check(ctx.handle, lib().bz_l0_opening_take_rows(handle, ctypes.byref(rh),
+                                                        ctypes.byref(data)))
+        owner = _RowsOwner(rh)
+        words = sz.n_queries * sz.row_len * 2
+        if words:
+            buf = (ctypes.c_uint64 * words).from_address(
+                ctypes.cast(data, ctypes.c_void_p).value)
+            buf._owner = owner
+            rows = np.frombuffer(buf, dtype=np.uint64).reshape(sz.n_queries, sz.row_len, 2)
+        else:
+            rows = np.zeros((0, sz.row_len, 2), np.uint64)
         self.sumcheck = [(sc[i, 0].copy(), sc[i, 1].copy()) for i in range(sz.n_sumcheck)]
         self.fold_nonces = [int(x) for x in fn[:sz.n_fold_nonces]]
         self.fold_challenges = ch[:k].copy()
@@ -89,7 +114,7 @@ class L0Opening:
         self.grinding_nonce = int(gn.value)
         self.queries = [int(x) for x in qs[:sz.n_queries]]
         self.alpha = al[:sz.n_alpha].copy()
-        self.opened_rows = rows[:sz.n_queries]
+        self.opened_rows = rows
         self.merkle_proof = proof[:sz.n_proof_hashes]
         ov = np.zeros((max(sz.n_ood_values, 1), 2), np.uint64)
         check(ctx.handle, lib().bz_l0_opening_ood_values(handle, ptr(ov)))

@@ -487,6 +487,27 @@ int bz_l0_opening_copy(const bz_l0_opening *o, uint64_t *sumcheck, uint64_t *fol
     return BZ_OK;
 }
 
+struct bz_rows {
+    std::vector<uint64_t, bzp::NoInitAlloc<uint64_t>> data;
+};
+
+int bz_l0_opening_take_rows(bz_l0_opening *o, bz_rows **rows, const uint64_t **data) {
+    if (!o || !rows || !data) return BZ_ERR_ARG;
+    bz_rows *r = new (std::nothrow) bz_rows();
+    if (!r) return BZ_ERR_NOMEM;
+    initial_rows(o);  // the helper thread writes o->initial
+    r->data = std::move(o->initial.rows.data);
+    o->initial.rows.data.clear();
+    *rows = r;
+    *data = r->data.data();
+    return BZ_OK;
+}
+
+int bz_rows_free(bz_rows *rows) {
+    delete rows;
+    return BZ_OK;
+}
+
 int bz_l0_opening_ood_values(const bz_l0_opening *o, uint64_t *values) {
     if (!o) return BZ_ERR_ARG;
     if (values && !o->ood_values.empty())

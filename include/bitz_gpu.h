@@ -386,6 +386,14 @@ int bz_l0_opening_sizes(const bz_l0_opening *o, bz_l0_sizes *sizes);
 int bz_l0_opening_copy(const bz_l0_opening *o, uint64_t *sumcheck, uint64_t *fold_nonces,
                        uint64_t *challenges, uint8_t root1[32], uint64_t *grinding_nonce,
                        uint64_t *queries, uint64_t *alpha, uint64_t *rows, uint8_t *proof);
+/* Move the opened rows out of the opening without a copy (the 9.7 MB of rows
+ * at 2^24): *data points at n_queries x row_len x 2 words, valid until
+ * bz_rows_free(*rows), independent of the opening's own lifetime.  Once
+ * taken, bz_l0_opening_copy writes no rows.  No counterpart in the
+ * reference (its opening returns the rows by value). */
+typedef struct bz_rows bz_rows;
+int bz_l0_opening_take_rows(bz_l0_opening *o, bz_rows **rows, const uint64_t **data);
+int bz_rows_free(bz_rows *rows);
 /* ood_samples1 x 2 words: the claimed evaluations, in transcript order. */
 int bz_l0_opening_ood_values(const bz_l0_opening *o, uint64_t *values);
 /* The level-1 commitment (owned by the opening). */
