@@ -523,35 +523,31 @@ int launch_sv_fold(const uint4 *d_packed, const uint4 *d_eq, size_t n, uint64_t 
     return 2;
 }
 
-// phi_from_words with phi_byte_tables (src/ligerito.rs:384-427): 16 byte
-// tables T[pos][v] = sum_{bit q of v} eq_r2[8 pos + q] in shared memory.
+// phi_from_words with phi_byte_tables (src/ligerito.rs:384-427): phi(y) =
+// sum over the set bits u of eq_hi[y] of eq_r2[u], a GF(2)-linear map of
+// eq_hi[y] whose image of bit u is eq_r2[u].  So it is a byte-table multiply:
+// the tables are expanded from those 128 images in the bank-conflict-free
+// layout of the NTT's and the folds' tables, and each word is one 16-lookup
+// table multiply.
 __global__ void __launch_bounds__(256) phi_kernel(const uint4 *eq_hi, uint64_t n,
                                                   const uint4 *eq_r2, uint4 *out) {
-    extern __shared__ uint4 tbl[];  // 16 * 256
-    for (int u = threadIdx.x; u < 16 * 256; u += blockDim.x) {
-        const int pos = u >> 8, v = u & 255;
-        uint4 acc = make_uint4(0, 0, 0, 0);
-        for (int q = 0; q < 8; ++q)
-            if ((v >> q) & 1) acc = gf_add(acc, eq_r2[8 * pos + q]);
-        tbl[u] = acc;
-    }
+    extern __shared__ uint4 smem[];
+    uint4 *bases = smem + kT16Entries;
+    for (int e = threadIdx.x; e < 128; e += blockDim.x)
+        bases[(e >> 3) * 9 + (e & 7)] = eq_r2[e];
     __syncthreads();
+    t16_expand(smem, bases, 1);
+    const char *T = reinterpret_cast<const char *>(smem);
+    T16Lane8 lc;
+    lc.init();
     for (uint64_t y = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; y < n;
-         y += (uint64_t)gridDim.x * blockDim.x) {
-        const uint4 w = eq_hi[y];
-        const uint32_t ws[4] = {w.x, w.y, w.z, w.w};
-        uint4 acc = make_uint4(0, 0, 0, 0);
-#pragma unroll
-        for (int pos = 0; pos < 16; ++pos) {
-            const uint32_t v = (ws[pos >> 2] >> (8 * (pos & 3))) & 0xff;
-            acc = gf_add(acc, tbl[pos * 256 + v]);
-        }
-        out[y] = acc;
-    }
+         y += (uint64_t)gridDim.x * blockDim.x)
+        out[y] = lc.mul(T, eq_hi[y]);
 }
 
 void init_fold_kernels() {
-    cudaFuncSetAttribute(phi_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, 65536);
+    cudaFuncSetAttribute(phi_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                         (int)kRTableSmem);
     cudaFuncSetAttribute(eq_split_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
                          (int)((2u << (kEqSplitMaxK / 2)) * sizeof(uint4)));
     cudaFuncSetAttribute(fold_and_msg_kernel<false>, cudaFuncAttributeMaxDynamicSharedMemorySize,
@@ -568,7 +564,7 @@ int launch_phi(const uint4 *d_eq_hi, size_t n, const uint4 *d_eq_r2, uint4 *d_ou
                cudaStream_t st, int num_sms) {
     const unsigned grid = (unsigned)std::max<uint64_t>(
         1, std::min<uint64_t>((n + 255) / 256, (uint64_t)2 * num_sms));
-    phi_kernel<<<grid, 256, 65536, st>>>(d_eq_hi, n, d_eq_r2, d_out);
+    phi_kernel<<<grid, 256, kRTableSmem, st>>>(d_eq_hi, n, d_eq_r2, d_out);
     return 1;
 }
 

@@ -26,19 +26,15 @@ __device__ __forceinline__ uint32_t t16_off(uint32_t k, uint32_t x) {
     return ((k >> 3) << 15) + (x << 7) + ((k & 7) << 4);
 }
 
-// Build the tables of n_tw twiddles (ts[i]) into tbl[i * 4096 ..].  `bases`
-// is kT16Bases * n_tw uint4 of scratch.  Called by all threads; syncs inside.
-// Thread u builds the 16 entries (k, hi * 16 + lo) of byte position
-// k = u mod 16: the 8 threads of a quarter-warp take 8 different byte
-// positions, so both their basis reads and their table writes fall in 8
-// different bank groups.
-static __device__ __noinline__ void t16_build(uint4 *tbl, uint4 *bases, const uint4 *ts, int n_tw) {
+// Expand 128 basis images per table (bases[i * kT16Bases + (e >> 3) * 9 +
+// (e & 7)] = image of bit e) into the byte tables tbl[i * 4096 ..]: T_k[x] =
+// XOR of the images of the set bits of x at byte position k.  Called by all
+// threads; syncs at the end.  Thread u builds the 16 entries (k, hi * 16 + lo)
+// of byte position k = u mod 16: the 8 threads of a quarter-warp take 8
+// different byte positions, so both their basis reads and their table writes
+// fall in 8 different bank groups.
+static __device__ __noinline__ void t16_expand(uint4 *tbl, const uint4 *bases, int n_tw) {
     const int tid = threadIdx.x, nthr = blockDim.x;
-    for (int j = tid; j < 128 * n_tw; j += nthr) {
-        const int i = j >> 7, e = j & 127;
-        bases[i * kT16Bases + (e >> 3) * 9 + (e & 7)] = gf_mul_xpow(ts[i], (uint32_t)e);
-    }
-    __syncthreads();
     for (int u = tid; u < 256 * n_tw; u += nthr) {
         const int i = u >> 8, k = u & 15, hi = (u >> 4) & 15;
         const uint4 *b = bases + i * kT16Bases + 9 * k;
@@ -61,6 +57,18 @@ static __device__ __noinline__ void t16_build(uint4 *tbl, uint4 *bases, const ui
             *reinterpret_cast<uint4 *>(tb + t16_off(k, (hi << 4) | lo)) = gf_add(H, L[lo]);
     }
     __syncthreads();
+}
+
+// Tables of multiplication by each twiddle ts[i] (the image of bit e is
+// ts[i] * X^e).  `bases` is kT16Bases * n_tw uint4 of scratch.  Called by all
+// threads; syncs inside.
+static __device__ __noinline__ void t16_build(uint4 *tbl, uint4 *bases, const uint4 *ts, int n_tw) {
+    for (int j = threadIdx.x; j < 128 * n_tw; j += blockDim.x) {
+        const int i = j >> 7, e = j & 127;
+        bases[i * kT16Bases + (e >> 3) * 9 + (e & 7)] = gf_mul_xpow(ts[i], (uint32_t)e);
+    }
+    __syncthreads();
+    t16_expand(tbl, bases, n_tw);
 }
 
 // Per-thread lookup offsets: step m reads byte position (m + s) mod 16.
