@@ -17,7 +17,7 @@ from dataclasses import dataclass
 
 import numpy as np
 
-from ._lib import check, lib, ptr
+from ._lib import BzError, check, lib, ptr
 from .pcs import Context, DeviceArray, ProverData, default_context
 from .transcript import Blake3Transcript
 
@@ -100,6 +100,8 @@ class L0Opening:
                                                         ctypes.byref(data)))
         owner = _RowsOwner(rh)
         words = sz.n_queries * sz.row_len * 2
+        if words and not data:
+            raise BzError(7, "opened rows missing")
         if words:
             buf = (ctypes.c_uint64 * words).from_address(
                 ctypes.cast(data, ctypes.c_void_p).value)

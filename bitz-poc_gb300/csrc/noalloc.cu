@@ -15,7 +15,11 @@
 // address, so the entry point resolves the real address once per device with
 // cudaGetSymbolAddress (on the first call made while that device is current)
 // and passes it to the kernels.  Make that first call on each device before
-// any stream capture.  All calls share the array and it keeps the previous
+// any stream capture.  The address and the kernels' shared-memory opt-in are
+// kept for the life of the process, so a cudaDeviceReset after the first
+// call on a device is not supported.  A launch error already pending on the
+// calling thread is reported (BZ_ERR_CUDA) before anything is launched and
+// left in place for its owner.  All calls share the array and it keeps the previous
 // call's contents: nothing in it has to start at zero (every block overwrites
 // its own slot and the final kernel reads only the slots of the current
 // launch), but calls that overlap on the GPU -- two streams, two threads --
@@ -49,6 +53,9 @@ extern "C" int bz_fold_and_msg_lsb_static(const uint64_t *d_f, const uint64_t *d
     if (!d_f || !d_b || !r || !d_nf || !d_nb || !d_msg) return BZ_ERR_ARG;
     if (!pow2(n) || n < 2) return BZ_ERR_SHAPE;  // n must be a power of two >= 2
     if (n > kMaxWords) return BZ_ERR_SHAPE;      // beyond 2^40 elements
+    // an error some earlier launch left pending belongs to its owner: report
+    // it without clearing it, so this call's own status cannot be mistaken
+    if (cudaPeekAtLastError() != cudaSuccess) return BZ_ERR_CUDA;
     int dev = 0;
     if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= kMaxDevices) {
         cudaGetLastError();
@@ -72,6 +79,8 @@ extern "C" int bz_fold_and_msg_lsb_static(const uint64_t *d_f, const uint64_t *d
             // the fold kernel keeps the challenge's byte tables in 66 KB of
             // dynamic shared memory; opt in for this device (no allocation)
             bz::init_fold_kernels();
+            // nothing was pending before (checked above), so this error is
+            // the attribute call's own
             if (cudaGetLastError() != cudaSuccess) return BZ_ERR_CUDA;
             g_partials_addr[dev] = (uint64_t *)p;
             g_num_sms[dev] = sms;
@@ -83,5 +92,6 @@ extern "C" int bz_fold_and_msg_lsb_static(const uint64_t *d_f, const uint64_t *d
                                 (uint32_t)(r[1] >> 32));
     bz::launch_fold_and_msg((const uint4 *)d_f, (const uint4 *)d_b, n, rr, (uint4 *)d_nf,
                             (uint4 *)d_nb, partials, d_msg, (cudaStream_t)stream, num_sms);
+    // read right after this call's own launches (no error was pending before)
     return cudaGetLastError() == cudaSuccess ? BZ_OK : BZ_ERR_CUDA;
 }

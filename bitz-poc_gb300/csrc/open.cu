@@ -493,9 +493,16 @@ struct bz_rows {
 
 int bz_l0_opening_take_rows(bz_l0_opening *o, bz_rows **rows, const uint64_t **data) {
     if (!o || !rows || !data) return BZ_ERR_ARG;
+    *rows = nullptr;
+    *data = nullptr;
+    const int rc = initial_rows(o);  // the helper thread writes o->initial
+    if (rc) return rc;
+    // the rows move out once: a second take, or rows that never arrived,
+    // find an array of the wrong size
+    const size_t want = o->queries.size() * (size_t)o->lanes * 2;
+    if (want && o->initial.rows.data.size() != want) return BZ_ERR_STATE;
     bz_rows *r = new (std::nothrow) bz_rows();
     if (!r) return BZ_ERR_NOMEM;
-    initial_rows(o);  // the helper thread writes o->initial
     r->data = std::move(o->initial.rows.data);
     o->initial.rows.data.clear();
     *rows = r;

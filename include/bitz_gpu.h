@@ -255,8 +255,12 @@ int bz_fold_and_msg_lsb(bz_ctx *ctx, const uint64_t *d_f, const uint64_t *d_b, s
  * device.  Enqueue only: synchronize the stream before reading outputs.  n
  * must be a power of two in [2, 2^40] (BZ_ERR_SHAPE otherwise).  The first
  * call on each device resolves the array's device address; make it before any
- * stream capture.  Calls that overlap on the GPU share the array and race.
- * Allocates nothing (no cudaMalloc, cudaFree or allocating library call). */
+ * stream capture.  That address is kept for the life of the process: a
+ * cudaDeviceReset after the first call on a device is not supported.  A
+ * launch error already pending on the calling thread gives BZ_ERR_CUDA before
+ * anything is launched and stays pending for its owner.  Calls that overlap
+ * on the GPU share the array and race.  Allocates nothing (no cudaMalloc,
+ * cudaFree or allocating library call). */
 int bz_fold_and_msg_lsb_static(const uint64_t *d_f, const uint64_t *d_b, size_t n,
                                const uint64_t r[2], uint64_t *d_nf, uint64_t *d_nb,
                                uint64_t *d_msg, void *stream);
@@ -389,8 +393,10 @@ int bz_l0_opening_copy(const bz_l0_opening *o, uint64_t *sumcheck, uint64_t *fol
 /* Move the opened rows out of the opening without a copy (the 9.7 MB of rows
  * at 2^24): *data points at n_queries x row_len x 2 words, valid until
  * bz_rows_free(*rows), independent of the opening's own lifetime.  Once
- * taken, bz_l0_opening_copy writes no rows.  No counterpart in the
- * reference (its opening returns the rows by value). */
+ * taken, bz_l0_opening_copy writes no rows.  The rows move out once: a
+ * second take returns BZ_ERR_STATE (and a failed row fetch its own error),
+ * with *rows and *data set to NULL.  No counterpart in the reference (its
+ * opening returns the rows by value). */
 typedef struct bz_rows bz_rows;
 int bz_l0_opening_take_rows(bz_l0_opening *o, bz_rows **rows, const uint64_t **data);
 int bz_rows_free(bz_rows *rows);

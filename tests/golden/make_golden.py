@@ -1,9 +1,12 @@
 """Regenerates the committed golden fixtures in tests/golden/.
 
-Run in a container that has the BitZ-PoC reference checkout at
-/root/reference and the ``cryptography`` package:
+Run where the BitZ-PoC reference checkout and the ``cryptography`` package
+are available, giving the checkout's root:
 
-    python tests/golden/make_golden.py
+    python tests/golden/make_golden.py --reference <path to BitZ-PoC>
+
+(the reference is read only for ``ghash``; the other fixtures need neither
+it nor the flag).
 
 Outputs (all small):
 
@@ -38,7 +41,7 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 REPO = os.path.dirname(os.path.dirname(HERE))
 sys.path.insert(0, REPO)
 
-RSP = "/root/reference/vendor/field/tests/vectors/gcm_encrypt_128.rsp"
+RSP_IN_REFERENCE = os.path.join("vendor", "field", "tests", "vectors", "gcm_encrypt_128.rsp")
 
 
 def parse_rsp(text):
@@ -66,10 +69,12 @@ def parse_rsp(text):
     return cases
 
 
-def make_ghash():
+def make_ghash(reference_root):
     from cryptography.hazmat.primitives.ciphers import Cipher, algorithms, modes
 
-    with open(RSP) as fh:
+    if not reference_root:
+        raise SystemExit("ghash needs --reference <path to the BitZ-PoC checkout>")
+    with open(os.path.join(reference_root, RSP_IN_REFERENCE)) as fh:
         cases = parse_rsp(fh.read())
     assert len(cases) == 525, len(cases)
     out = []
@@ -182,12 +187,18 @@ def add_root(lm, r, lb, kind, seed):
 
 
 if __name__ == "__main__":
-    if sys.argv[1:2] == ["root"]:
-        add_root(*[int(x) for x in sys.argv[2:7]])
+    args = sys.argv[1:]
+    reference = None
+    if "--reference" in args:
+        i = args.index("--reference")
+        reference = args[i + 1]
+        del args[i:i + 2]
+    if args[:1] == ["root"]:
+        add_root(*[int(x) for x in args[1:6]])
         sys.exit(0)
-    which = sys.argv[1:] or ["ghash", "chacha", "cmt1", "roots"]
+    which = args or ["ghash", "chacha", "cmt1", "roots"]
     if "ghash" in which:
-        make_ghash()
+        make_ghash(reference)
     if "chacha" in which:
         make_chacha()
     if "cmt1" in which:

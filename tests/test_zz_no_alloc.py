@@ -4,9 +4,11 @@ It serves callers that cannot allocate device memory -- a prover host whose
 runtime reserved the GPU's memory for its own pool, or a fold loop that
 cannot pay for cudaMalloc's synchronisation -- by keeping the fold's per-block
 scratch in a fixed device array.  This test calls it through the C ABI and
-checks it against the allocating entry point (bz_fold_and_msg_lsb) on two
-calls in a row, so stale scratch from the first call would show up in the
-second.  Results are exact (bit-identical) field values.
+checks it against the allocating entry point (bz_fold_and_msg_lsb) on calls
+in a row, so stale scratch from an earlier call would show up in a later one,
+and against the CPU oracle's fold_and_msg_lsb directly, so a fault the two
+GPU paths shared would show up too.  Results are exact (bit-identical) field
+values.
 
 The file name sorts last so that a run stopping at its first failure has
 already run every other test.
@@ -56,20 +58,26 @@ def _run_pair(L, ctx, f, b, r):
     return host, u0, u2, msg
 
 
-def test_static_fold_matches_allocating_fold_twice(ctx):
+def test_static_fold_matches_allocating_fold_twice(ctx, oracle):
     from bitz_gb300 import _lib
 
     L = _lib.lib()
     rng = np.random.default_rng(2024)
-    # two calls in a row: a large fold, then a small one whose few blocks
-    # must not pick up the first call's partial sums
-    for n in (1 << 18, 1 << 10):
+    # calls in a row: a large fold, then smaller ones whose few blocks must
+    # not pick up an earlier call's partial sums; n = 2 folds one pair (one
+    # thread, empty message), n = 4 leaves a single folded pair
+    for n in (1 << 18, 1 << 10, 2, 4):
         f = rng.integers(0, 2**64, (n, 2), dtype=np.uint64)
         b = rng.integers(0, 2**64, (n, 2), dtype=np.uint64)
         r = rng.integers(0, 2**64, 2, dtype=np.uint64)
         (nf, nb, nf_s, nb_s), u0, u2, msg = _run_pair(L, ctx, f, b, r)
         assert (nf_s == nf).all() and (nb_s == nb).all()
         assert (msg[:2] == u0).all() and (msg[2:] == u2).all()
+        if n <= 1 << 10:
+            # the CPU oracle, independently of either GPU path
+            ef, eb, e0, e2 = oracle.fold_and_msg_lsb(f, b, r)
+            assert (nf_s == ef).all() and (nb_s == eb).all()
+            assert (msg[:2] == e0).all() and (msg[2:] == e2).all()
 
 
 def test_static_fold_rejects_bad_sizes(ctx):
