@@ -26,3 +26,4 @@ from .opening import L0Config, L0Opening, LigeritoConfig, open_l0, prove  # noqa
 from . import codec  # noqa: F401,E402
 from .binary_pcs import BinaryPcs, BitMleOpening, Round0Prover  # noqa: F401,E402
 from . import ingest  # noqa: F401,E402
+from . import shard  # noqa: F401,E402

@@ -136,6 +136,10 @@ _SIGS = {
     "bz_pack_columns_from_rows": (_I, [_P, _P, _U32, _U32, _P]),
     "bz_rows_from_packed_cols": (_I, [_P, _P, _U32, _U32, _P]),
     "bz_commit_rows": (_I, [_P, _P, _U32, _U32, _U32, _U32, _U32, _PP, _P]),
+    "bz_commit_shard": (_I, [_P, _P, _S, ctypes.POINTER(Params), _U32, _U32, _PP]),
+    "bz_commit_shard_device": (_I, [_P, _P, _S, ctypes.POINTER(Params), _U32, _U32, _PP]),
+    "bz_commitment_leaf_cvs": (_I, [_P, _P, _S]),
+    "bz_merkle_from_shards": (_I, [_P, _P, _U32, ctypes.POINTER(Params), _PP, _P]),
     "bz_autotune": (_I, [_P, ctypes.POINTER(Params), _I, ctypes.POINTER(_U32)]),
     "bz_schedule_get": (_I, [_P, ctypes.POINTER(Params), ctypes.POINTER(_U32)]),
     "bz_schedule_set": (_I, [_P, ctypes.POINTER(Params), _U32]),

@@ -16,6 +16,10 @@ struct Shape {
     int log_inv_rate = 0;   // r
     int log_lanes = 0;      // log_batch_size (a)
     int hash_kind = 1;      // 0 sha256, 1 blake3
+    // BLAKE3 chunk counter of lane 0's chunk inside its leaf: 0 for a whole
+    // commit; rank * (lanes / 64) for one rank's lanes of a lane-sharded
+    // commit, whose "leaves" are then the CVs of its aligned run of chunks
+    uint64_t chunk0 = 0;
     int log_dim() const { return log_msg_len - log_lanes; }        // b
     int k_code() const { return log_dim() + log_inv_rate; }        // ell
     size_t msg_words() const { return (size_t)1 << log_msg_len; }
@@ -98,6 +102,11 @@ int launch_commit_pipelined(const Shape &s, uint32_t schedule, const uint4 *d_ms
                             uint8_t *d_tree, const uint4 *d_tw, cudaStream_t st,
                             cudaStream_t aux, cudaEvent_t *ev, int num_sms, LaunchLog *log);
 
+// Leaf CVs of a lane-sharded BLAKE3 commit: leaf p = the merge of the world
+// ranks' subtree CVs cvs[rank * n_leaves + p] (world a power of two), written
+// to tree[0 .. n_leaves).
+int launch_combine_shard_cvs(const uint8_t *d_cvs, uint32_t world, uint64_t n_leaves,
+                             uint8_t *d_tree, cudaStream_t st);
 // Merkle tree over the codeword rows (leaves = positions).  d_scratch must hold
 // merkle_scratch_bytes(s).  Returns kernels launched.
 size_t merkle_scratch_bytes(const Shape &s);

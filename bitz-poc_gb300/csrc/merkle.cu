@@ -28,10 +28,10 @@ namespace bz {
 // ---------------------------------------------------------------------------
 __global__ void __launch_bounds__(256) b3_leaves_chunked(const uint4 *cw, int log_lanes,
                                                          uint64_t n_chunks, uint32_t *tree_leaves,
-                                                         int log_c) {
+                                                         int log_c, uint64_t chunk0) {
     __shared__ uint32_t cvs[256][9];  // padded rows
     const uint64_t chunk = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
-    const uint32_t c_in_leaf = (uint32_t)(chunk & ((1u << log_c) - 1));
+    const uint64_t c_in_leaf = chunk0 + (chunk & ((1u << log_c) - 1));
     uint32_t cv[8];
 #pragma unroll
     for (int i = 0; i < 8; ++i) cv[i] = kIV[i];
@@ -167,10 +167,11 @@ __global__ void __launch_bounds__(kTreeSmallMax) b3_tree_small(const uint4 *cw, 
 }
 
 // Generic BLAKE3 chunk CVs into scratch (leaves longer than 256 chunks).
-__global__ void b3_chunk_cvs(const uint4 *cw, uint64_t n_chunks, int log_c, uint32_t *out) {
+__global__ void b3_chunk_cvs(const uint4 *cw, uint64_t n_chunks, int log_c, uint32_t *out,
+                             uint64_t chunk0) {
     const uint64_t chunk = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (chunk >= n_chunks) return;
-    const uint32_t c_in_leaf = (uint32_t)(chunk & ((1ull << log_c) - 1));
+    const uint64_t c_in_leaf = chunk0 + (chunk & ((1ull << log_c) - 1));
     uint32_t cv[8];
 #pragma unroll
     for (int i = 0; i < 8; ++i) cv[i] = kIV[i];
@@ -371,7 +372,7 @@ int launch_leaves_range(const Shape &s, const uint4 *d_cw, uint8_t *d_tree, uint
             const uint64_t n_chunks = n << log_c;
             const unsigned t = leaf_threads(n_chunks, log_c, num_sms);
             b3_leaves_chunked<<<(unsigned)((n_chunks + t - 1) / t), t, 0, st>>>(
-                cw, s.log_lanes, n_chunks, leaves, log_c);
+                cw, s.log_lanes, n_chunks, leaves, log_c, s.chunk0);
         }
     } else {
         sha_leaves<<<(unsigned)((n + 127) / 128), 128, 0, st>>>(cw, s.log_lanes, n, leaves);
@@ -447,7 +448,7 @@ int launch_merkle(const Shape &s, const uint4 *d_cw, uint8_t *d_tree, uint8_t *d
             const uint64_t n_chunks = n_leaves << log_c;
             const unsigned t = leaf_threads(n_chunks, log_c, num_sms);
             b3_leaves_chunked<<<(unsigned)((n_chunks + t - 1) / t), t, 0, st>>>(
-                d_cw, s.log_lanes, n_chunks, tree, log_c);
+                d_cw, s.log_lanes, n_chunks, tree, log_c, s.chunk0);
             mark("b3_leaves_chunked");
             ++launches;
         } else {
@@ -455,7 +456,7 @@ int launch_merkle(const Shape &s, const uint4 *d_cw, uint8_t *d_tree, uint8_t *d
             const uint64_t n_chunks = n_leaves << log_c;
             uint32_t *cvs = reinterpret_cast<uint32_t *>(d_scratch);
             b3_chunk_cvs<<<(unsigned)((n_chunks + 255) / 256), 256, 0, st>>>(d_cw, n_chunks,
-                                                                           log_c, cvs);
+                                                                           log_c, cvs, s.chunk0);
             mark("b3_chunk_cvs");
             ++launches;
             // reduce chunk CVs to leaf CVs: levels inside the scratch area,
@@ -485,6 +486,49 @@ int launch_merkle(const Shape &s, const uint4 *d_cw, uint8_t *d_tree, uint8_t *d
     }
     launches += launch_levels(tree, n_leaves, s.hash_kind, st, log);
     return launches;
+}
+
+// ---------------------------------------------------------------------------
+// Leaves of a lane-sharded BLAKE3 commit: one thread per position merges the
+// world ranks' subtree CVs left to right with BLAKE3's CV stack (a subtree of
+// 2^j ranks is merged with its left neighbour of the same size), which for a
+// power-of-two world is the perfect binary tree of PARENT merges the leaf's
+// own chunk tree has above those subtrees (merkle.rs:160-201).
+// ---------------------------------------------------------------------------
+constexpr int kMaxShardLevels = 11;  // world <= 1024
+__global__ void b3_combine_shard_cvs(const uint32_t *cvs, uint32_t world, uint64_t n_leaves,
+                                     uint32_t *leaves) {
+    const uint64_t p = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (p >= n_leaves) return;
+    uint32_t stack[kMaxShardLevels][8];
+    int depth = 0;
+    for (uint32_t r = 0; r < world; ++r) {
+        uint32_t cv[8];
+#pragma unroll
+        for (int i = 0; i < 8; ++i) cv[i] = cvs[((uint64_t)r * n_leaves + p) * 8 + i];
+        // merge while the subtree just completed has a left sibling of equal
+        // size: the number of trailing one bits of r
+        for (uint32_t m = r; m & 1; m >>= 1) {
+            uint32_t o[8];
+            b3_parent(stack[--depth], cv, o);
+#pragma unroll
+            for (int i = 0; i < 8; ++i) cv[i] = o[i];
+        }
+#pragma unroll
+        for (int i = 0; i < 8; ++i) stack[depth][i] = cv[i];
+        ++depth;
+    }
+#pragma unroll
+    for (int i = 0; i < 8; ++i) leaves[p * 8 + i] = stack[0][i];
+}
+
+int launch_combine_shard_cvs(const uint8_t *d_cvs, uint32_t world, uint64_t n_leaves,
+                             uint8_t *d_tree, cudaStream_t st) {
+    if (world == 0 || (world & (world - 1)) || world > (1u << (kMaxShardLevels - 1))) return 0;
+    b3_combine_shard_cvs<<<(unsigned)((n_leaves + 127) / 128), 128, 0, st>>>(
+        reinterpret_cast<const uint32_t *>(d_cvs), world, n_leaves,
+        reinterpret_cast<uint32_t *>(d_tree));
+    return 1;
 }
 
 // ---------------------------------------------------------------------------

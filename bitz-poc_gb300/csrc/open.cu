@@ -378,6 +378,7 @@ int open_level0(bz_ctx *ctx, bz_transcript *transcript, bz_commitment *c0,
         return BZ_ERR_ARG;
     *out = nullptr;
     if (c0->ctx != ctx) return bz::set_msg(ctx, BZ_ERR_ARG, "commitment of another context");
+    if (!c0->d_cw) return bz::set_msg(ctx, BZ_ERR_STATE, "tree-only commitment: no codeword");
     const bz::Shape &s = c0->shape;
     const uint32_t log_n = (uint32_t)s.log_msg_len, k = cfg->initial_k;
     if (k != (uint32_t)s.log_lanes)

@@ -188,14 +188,16 @@ uint32_t schedule_for(bz_ctx *ctx, const Shape &s) {
 static std::mutex g_handles_mu;
 static std::set<const bz_commitment *> g_handles;
 
-// Allocate a commitment's resident buffers (budgeted).
-int alloc_commitment(bz_ctx *ctx, const Shape &s, bz_commitment **out) {
+// Allocate a commitment's resident buffers (budgeted).  Without a codeword
+// the handle holds only a tree (the global tree of a lane-sharded commit,
+// whose codeword stays split over the ranks).
+int alloc_commitment(bz_ctx *ctx, const Shape &s, bz_commitment **out, bool with_codeword) {
     bz_commitment *c = new bz_commitment();
     c->ctx = ctx;
     c->shape = s;
-    c->cw_bytes = s.cw_words() * 16;
+    c->cw_bytes = with_codeword ? s.cw_words() * 16 : 0;
     c->tree_bytes = s.tree_nodes() * 32;
-    int rc = dev_alloc(ctx, c->cw_bytes, (void **)&c->d_cw, true);
+    int rc = with_codeword ? dev_alloc(ctx, c->cw_bytes, (void **)&c->d_cw, true) : BZ_OK;
     if (rc) {
         delete c;
         return rc;
@@ -269,6 +271,7 @@ int launch_commit_kernels(bz_ctx *ctx, const Shape &s, uint32_t schedule, const 
 int commitment_rows_on(bz_commitment *c, const uint64_t *positions, size_t q, uint64_t *out,
                        cudaStream_t st) {
     bz_ctx *ctx = c->ctx;
+    if (!c->d_cw) return set_msg(ctx, BZ_ERR_STATE, "tree-only commitment: no codeword");
     const uint64_t n_pos = c->shape.n_leaves();
     for (size_t i = 0; i < q; ++i)
         if (positions[i] >= n_pos) return set_msg(ctx, BZ_ERR_ARG, "position out of range");
@@ -715,6 +718,7 @@ int bz_commitment_device_ptrs(const bz_commitment *c, const uint64_t **d_codewor
 int bz_commitment_copy_codeword(bz_commitment *c, uint64_t *out, size_t n_words) {
     if (!c || !out) return BZ_ERR_ARG;
     bz_ctx *ctx = c->ctx;
+    if (!c->d_cw) return set_msg(ctx, BZ_ERR_STATE, "tree-only commitment: no codeword");
     if (n_words != c->shape.cw_words()) return set_msg(ctx, BZ_ERR_ARG, "codeword size");
     BZ_CUDA(ctx, cudaMemcpyAsync(out, c->d_cw, n_words * 16, cudaMemcpyDeviceToHost, ctx->stream));
     BZ_CUDA(ctx, cudaStreamSynchronize(ctx->stream));

@@ -103,7 +103,8 @@ int commitment_multiproof_on(bz_commitment *c, const uint64_t *positions, size_t
                              size_t cap, size_t *n_hashes, cudaStream_t st);
 int get_twiddles(bz_ctx *ctx, int ell, const uint4 **out);
 uint32_t schedule_for(bz_ctx *ctx, const Shape &s);
-int alloc_commitment(bz_ctx *ctx, const Shape &s, bz_commitment **out);
+int alloc_commitment(bz_ctx *ctx, const Shape &s, bz_commitment **out,
+                     bool with_codeword = true);
 int enqueue_commit(bz_ctx *ctx, const Shape &s, const uint4 *d_msg, bz_commitment *c,
                    cudaStream_t st, uint32_t schedule);
 int fetch_root(bz_commitment *c);

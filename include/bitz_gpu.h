@@ -135,6 +135,40 @@ int bz_commitment_multiproof(bz_commitment *c, const uint64_t *positions, size_t
                              uint8_t *out, size_t cap, size_t *n_hashes);
 int bz_commitment_free(bz_commitment *c);
 
+/* ---- lane-sharded BLAKE3 commit (one commit over several GPUs) ----------- */
+/* No counterpart in the reference, which commits on one machine.  It splits
+ * flock-core's commit (commit.rs:180-315) by lanes: every lane's NTT is
+ * independent (flock-core/src/ntt/additive_ntt_f128.rs:176-191) and a BLAKE3
+ * leaf is the tree over its 1 KiB chunks of 64 lanes, the chunk's index in
+ * the leaf being its counter (flock-core/src/merkle.rs:160-201).
+ *
+ * Rank `rank` of `world` (a power of two; 2^log_batch_size / world >= 64
+ * lanes; BLAKE3 only, else BZ_ERR_SHAPE) commits its lanes
+ * [rank Ls, (rank+1) Ls), Ls = 2^log_batch_size / world, from its message
+ * shard msg_shard[col * Ls + j] = msg[col * 2^log_batch_size + rank * Ls + j]
+ * (n_words = 2^log_msg_len / world).  `params` are the whole commit's.  The
+ * returned handle holds the shard's codeword (its lanes of every position,
+ * cw[pos * Ls + j]: bz_commitment_rows gives the rank's slice of opened rows)
+ * and as its leaves the CV of each position's run of chunks
+ * (bz_commitment_leaf_cvs); its own root means nothing.  Synchronous. */
+int bz_commit_shard(bz_ctx *ctx, const uint64_t *msg_shard, size_t n_words,
+                    const bz_params *params, uint32_t world, uint32_t rank, bz_commitment **out);
+/* Same with the shard in device memory; enqueue only. */
+int bz_commit_shard_device(bz_ctx *ctx, const uint64_t *d_msg_shard, size_t n_words,
+                           const bz_params *params, uint32_t world, uint32_t rank,
+                           bz_commitment **out);
+/* The n_leaves x 32-byte leaves of a commitment's tree (a shard's per-position
+ * chunk-run CVs: what the ranks exchange, an all-gather of 32 bytes per
+ * position per rank). */
+int bz_commitment_leaf_cvs(bz_commitment *c, uint8_t *out, size_t n_leaves);
+/* The whole commit's tree from every rank's leaf CVs (host, world x n_leaves
+ * x 32 bytes in rank order): each leaf CV is the merge of its position's world
+ * CVs, then the Merkle levels.  *out is a tree-only handle (root, copy_tree,
+ * multiproof; its codeword stays split over the ranks, so bz_commitment_rows
+ * and copy_codeword return BZ_ERR_STATE); root receives the commit's root. */
+int bz_merkle_from_shards(bz_ctx *ctx, const uint8_t *cvs, uint32_t world,
+                          const bz_params *params, bz_commitment **out, uint8_t root[32]);
+
 /* Phase timing: one commit as bz_commit_device with a CUDA event after every
  * kernel; ms[i] is the device time of launch i and names + 32*i its kernel
  * name (NUL terminated).  At most cap entries; *count receives the number of

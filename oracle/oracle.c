@@ -605,6 +605,26 @@ void orc_blake3_leaf_cv(const uint8_t *data, size_t len, uint8_t out[32]) {
     cv_to_bytes(w, out);
 }
 
+/* Non-root CV of a power-of-two run of whole chunks that starts at chunk
+ * `first_chunk` of a larger input (the BLAKE3 specification's tree: a chunk's
+ * counter is its index in the whole input, and an aligned power-of-two run of
+ * chunks is one node of the whole input's tree, merged non-root like the
+ * PARENT nodes of merkle.rs:160-201).  One row of a lane shard is such a run
+ * inside its leaf. */
+void orc_blake3_subtree_cv(const uint8_t *data, size_t len, uint64_t first_chunk,
+                           uint8_t out[32]) {
+    uint32_t w[8];
+    b3_subtree(data, len, first_chunk, 0, w);
+    cv_to_bytes(w, out);
+}
+
+/* orc_blake3_subtree_cv of each of n_rows consecutive rows of row_len bytes. */
+void orc_blake3_rows_subtree_cvs(const uint8_t *rows, size_t n_rows, size_t row_len,
+                                 uint64_t first_chunk, uint8_t *out) {
+    for (size_t i = 0; i < n_rows; ++i)
+        orc_blake3_subtree_cv(rows + i * row_len, row_len, first_chunk, out + 32 * i);
+}
+
 void orc_blake3_parent_cv(const uint8_t l[32], const uint8_t r[32], uint8_t out[32]) {
     uint32_t lw[8], rw[8], o[8];
     cv_from_bytes(l, lw);
@@ -656,6 +676,18 @@ void orc_merkle_tree(const uint8_t *data, size_t data_len, size_t num_leaves, in
     while (len > 1) {
         struct pairs_ctx pc = {tree + 32 * rd, tree + 32 * (rd + len), kind};
         parallel_for(len / 2, len >= 1024 ? n_threads : 1, pairs_range, &pc);
+        rd += len;
+        len >>= 1;
+    }
+}
+
+/* The levels above given leaf hashes (tree[0 .. num_leaves) already holds
+ * the leaves): the same flat layout and pair hashing as orc_merkle_tree. */
+void orc_merkle_tree_from_leaves(uint8_t *tree, size_t num_leaves, int kind) {
+    size_t rd = 0, len = num_leaves;
+    while (len > 1) {
+        struct pairs_ctx pc = {tree + 32 * rd, tree + 32 * (rd + len), kind};
+        parallel_for(len / 2, 1, pairs_range, &pc);
         rd += len;
         len >>= 1;
     }

@@ -57,6 +57,12 @@ void orc_sha256(const uint8_t *data, size_t len, uint8_t out[32]);
 void orc_blake3_hash(const uint8_t *data, size_t len, uint8_t out[32]);
 /* Hasher::new().update(data).finalize_non_root() */
 void orc_blake3_leaf_cv(const uint8_t *data, size_t len, uint8_t out[32]);
+/* Non-root CV of whole chunks starting at chunk `first_chunk` of a larger
+ * input (len a power-of-two number of 1 KiB chunks) */
+void orc_blake3_subtree_cv(const uint8_t *data, size_t len, uint64_t first_chunk,
+                           uint8_t out[32]);
+void orc_blake3_rows_subtree_cvs(const uint8_t *rows, size_t n_rows, size_t row_len,
+                                 uint64_t first_chunk, uint8_t *out);
 /* merge_subtrees_non_root(l, r, Mode::Hash) */
 void orc_blake3_parent_cv(const uint8_t l[32], const uint8_t r[32], uint8_t out[32]);
 
@@ -75,6 +81,8 @@ void orc_hash_pair(const uint8_t l[32], const uint8_t r[32], int kind, uint8_t o
 void orc_merkle_tree(const uint8_t *data, size_t data_len, size_t num_leaves, int kind,
                      uint8_t *tree /* (2*num_leaves-1)*32 */, int n_threads);
 /* returns number of hashes written to out (caller sizes out for q*depth) */
+/* parent levels above the leaves already in tree[0 .. num_leaves) */
+void orc_merkle_tree_from_leaves(uint8_t *tree, size_t num_leaves, int kind);
 size_t orc_merkle_multi_proof(const uint8_t *tree, size_t num_leaves,
                               const uint64_t *positions, size_t q, uint8_t *out);
 int orc_verify_merkle_multi_proof(const uint8_t root[32], size_t num_leaves,

@@ -64,9 +64,12 @@ def _declare(L):
         "orc_pow_first_nonce": (_U64, [_P, _S, _U64, _U64, ctypes.c_uint]),
         "orc_blake3_leaf_cv": (None, [_P, _S, _P]),
         "orc_blake3_parent_cv": (None, [_P, _P, _P]),
+        "orc_blake3_subtree_cv": (None, [_P, _S, _U64, _P]),
+        "orc_blake3_rows_subtree_cvs": (None, [_P, _S, _S, _U64, _P]),
         "orc_hash_leaf": (None, [_P, _S, _I, _P]),
         "orc_hash_pair": (None, [_P, _P, _I, _P]),
         "orc_merkle_tree": (None, [_P, _S, _S, _I, _P, _I]),
+        "orc_merkle_tree_from_leaves": (None, [_P, _S, _I]),
         "orc_merkle_multi_proof": (_S, [_P, _S, _P, _S, _P]),
         "orc_verify_merkle_multi_proof": (_I, [_P, _S, _P, _P, _S, _P, _S, _I]),
         "orc_commit": (_I, [_P, _I, _I, _I, _I, _P, _P, _P, _I]),
@@ -213,6 +216,25 @@ def blake3_leaf_cv(data: bytes) -> bytes:
     return out.tobytes()
 
 
+def blake3_subtree_cv(data: bytes, first_chunk: int) -> bytes:
+    """Non-root CV of whole 1 KiB chunks that start at chunk `first_chunk` of a
+    larger input (a power-of-two run of chunks: one node of that input's tree)."""
+    a = _bytes_in(data)
+    out = np.zeros(32, np.uint8)
+    lib().orc_blake3_subtree_cv(_p(a), len(data), first_chunk, _p(out))
+    return out.tobytes()
+
+
+def rows_subtree_cvs(rows: np.ndarray, first_chunk: int) -> np.ndarray:
+    """blake3_subtree_cv of every row of `rows` ((n, row_words, 2) uint64)."""
+    rows = np.ascontiguousarray(rows, np.uint64)
+    n = rows.shape[0]
+    row_len = rows[0].nbytes if n else 0
+    out = np.zeros((n, 32), np.uint8)
+    lib().orc_blake3_rows_subtree_cvs(_p(rows), n, row_len, first_chunk, _p(out))
+    return out
+
+
 def blake3_parent_cv(l: bytes, r: bytes) -> bytes:
     out = np.zeros(32, np.uint8)
     lib().orc_blake3_parent_cv(_p(_bytes_in(l)), _p(_bytes_in(r)), _p(out))
@@ -277,6 +299,61 @@ def commit(msg: np.ndarray, log_inv_rate: int, log_batch_size: int, hash_kind: i
     if rc != 0:
         raise ValueError("bad commit shape")
     return cw, tree, root.tobytes()
+
+
+def merkle_tree_from_leaves(leaves: np.ndarray, kind: int) -> np.ndarray:
+    """Flat tree (2n-1, 32) over n given leaf hashes."""
+    leaves = np.asarray(leaves, np.uint8).reshape(-1, 32)
+    n = leaves.shape[0]
+    tree = np.zeros((2 * n - 1, 32), np.uint8)
+    tree[:n] = leaves
+    lib().orc_merkle_tree_from_leaves(_p(tree), n, kind)
+    return tree
+
+
+# ---- lane-sharded BLAKE3 commit ---------------------------------------------
+# Every lane's NTT is independent (flock-core/src/ntt/additive_ntt_f128.rs:
+# 176-191) and a leaf's BLAKE3 CV is a tree over its 1 KiB chunks, each chunk
+# being 64 lanes of one position with its index in the leaf as the counter
+# (flock-core/src/merkle.rs:160-201).  So rank `rank` of `world` (a power of
+# two, L / world >= 64 lanes) encodes lanes [rank L/world, (rank+1) L/world)
+# as a commit of its own, and reduces each of its rows to the CV of the aligned
+# run of chunks it holds; every leaf CV is then the merge of the world CVs of
+# its position.
+
+
+def lane_shard(msg: np.ndarray, log_batch_size: int, world: int, rank: int) -> np.ndarray:
+    """Rank's message shard: msg[col * L + lane] for its lanes, compact."""
+    L = 1 << log_batch_size
+    Ls = L // world
+    m = np.asarray(msg, np.uint64).reshape(-1, L, 2)
+    return np.ascontiguousarray(m[:, rank * Ls:(rank + 1) * Ls]).reshape(-1, 2)
+
+
+def commit_lane_shard(msg_shard: np.ndarray, log_inv_rate: int, log_batch_size: int,
+                      world: int, rank: int):
+    """(shard codeword (positions x L/world lanes), per-position subtree CVs)."""
+    ls = log_batch_size - (world.bit_length() - 1)
+    if world & (world - 1) or ls < 6:
+        raise ValueError("world must be a power of two leaving >= 64 lanes per rank")
+    cw, _, _ = commit(msg_shard, log_inv_rate, ls, BLAKE3)
+    rows = cw.reshape(-1, 1 << ls, 2)
+    return cw, rows_subtree_cvs(rows, rank * ((1 << ls) // 64))
+
+
+def merkle_from_shard_cvs(cvs: np.ndarray):
+    """Tree and root from the ranks' subtree CVs ((world, positions, 32), rank order)."""
+    cvs = np.asarray(cvs, np.uint8)
+    level = [cvs[r] for r in range(cvs.shape[0])]
+    while len(level) > 1:
+        nxt = []
+        for i in range(0, len(level), 2):
+            a, b = level[i], level[i + 1]
+            nxt.append(np.stack([np.frombuffer(blake3_parent_cv(a[p].tobytes(), b[p].tobytes()),
+                                               np.uint8) for p in range(a.shape[0])]))
+        level = nxt
+    tree = merkle_tree_from_leaves(level[0], BLAKE3)
+    return tree, tree[-1].tobytes()
 
 
 def partial_eval_lsb(evals: np.ndarray, rs: np.ndarray) -> np.ndarray:
