@@ -63,7 +63,9 @@ NCU_TRAFFIC_PER_CW_BYTE = {
 
 def table_pass_lookup_bytes(kernel: str, layer: int, log_positions_lanes: int) -> int | None:
     """Shared-memory bytes read by the twiddle multiplies of one table pass
-    over 2^log_positions_lanes codeword elements starting at `layer`.
+    over 2^log_positions_lanes codeword elements starting at `layer` (16
+    lookups of 16 B per product with either table layout: sixteen tables of
+    one byte position each, or eight tables serving both 64-bit halves).
 
     A radix-4 pass multiplies each quad 4 times (t_o twice, then t_a and
     t_b), a radix-2 pass each pair once.  Block 0 of every layer has a zero
@@ -72,6 +74,12 @@ def table_pass_lookup_bytes(kernel: str, layer: int, log_positions_lanes: int) -
     n = 1 << log_positions_lanes
     if kernel.endswith("_nw"):
         return None   # compact 4-byte tables for narrow twiddles: not this model
+    if kernel.startswith("ntt_pass8"):
+        # radix-8: 12 products per octet; block 0's seven zero twiddles skip
+        # 4 + 2 + 1 of them in the first super-block
+        octets = n // 8
+        muls = 12 * octets - 7 * (octets >> layer)
+        return muls * T16_BYTES_PER_MUL
     if kernel.startswith("ntt_table_pass2"):
         quads = n // 4
         muls = 4 * quads - 3 * (quads >> layer)
@@ -707,17 +715,59 @@ def _geometric_sizes(rng, n, lo=14, hi=26, q=0.97):
     return rng.choice(ks, size=n, p=w)
 
 
+def _bench_plain_mix(ctx, bz, L, _lib, hp, sizes, params):
+    """The plain one-at-a-time GPU path over a request list: per request a
+    synchronous bz_commit of its host message (H2D inside), its opened rows
+    and multi-proof at positions [0, 1, 7], then free.  Returns (elements per
+    second, {log2 size: median per-request ms})."""
+    import ctypes
+
+    pos = np.array([0, 1, 7], np.uint64)
+    per_size = {}
+    total = 0
+    ctx.synchronize()
+    t0 = time.perf_counter()
+    for k in sizes:
+        k = int(k)
+        p = params[k]
+        pc = p.to_c()
+        t1 = time.perf_counter()
+        h = ctypes.c_void_p()
+        root = (ctypes.c_uint8 * 32)()
+        _lib.check(ctx.handle, L.bz_commit(ctx.handle, hp, 1 << k, ctypes.byref(pc),
+                                           ctypes.byref(h), root))
+        rows = np.empty((3, p.num_ntts(), 2), np.uint64)
+        _lib.check(ctx.handle, L.bz_commitment_rows(h, _lib.ptr(pos), 3, _lib.ptr(rows)))
+        depth = p.k_code()
+        proof = np.empty((3 * depth, 32), np.uint8)
+        n = ctypes.c_size_t()
+        _lib.check(ctx.handle, L.bz_commitment_multiproof(h, _lib.ptr(pos), 3, _lib.ptr(proof),
+                                                          3 * depth, ctypes.byref(n)))
+        L.bz_commitment_free(h)
+        per_size.setdefault(k, []).append((time.perf_counter() - t1) * 1e3)
+        total += 1 << k
+    wall = time.perf_counter() - t0
+    return total / wall, {k: statistics.median(v) for k, v in per_size.items()}
+
+
 def _bench_serve(ctx, bz, args, plain_rate=None):
     """Poisson commit-then-open requests with log2 sizes from a truncated
     geometric on [14, 26], admitted by free HBM (continuous batching); the
-    arrival rate is swept to saturation.  Reports throughput and p50/p99
-    submit-to-opened latency per rate.  Offered load is relative to
-    ``plain_rate``, the one-at-a-time GPU commit rate of the C4 size mix
-    measured in the same run (4e9 elems/s when that leg is skipped).  The
-    saturating point (1.5 x) serves ``--serve-requests`` requests (10k by
-    default); the lighter loads a tenth of that.  Each request is one
-    ``submit_commit_open`` (the server queues the opening when the commit
-    completes) and the request loop reacts to the server's completion queue."""
+    arrival rate is swept to saturation.  Each request is one
+    ``submit_commit_open`` of a host message (the server queues the opening,
+    rows + multi-proof at 3 positions, when the commit completes) and the
+    request loop reacts to the server's completion queue.
+
+    The baseline is the plain one-at-a-time GPU path on the same mix: the
+    same kind of request list served by synchronous bz_commit + rows +
+    multi-proof calls (``plain_same_mix``).  Offered loads are fractions of
+    that plain rate, so load 1.0 is what the plain path can just sustain.
+    Besides throughput and p50/p99 submit-to-opened latency, each rate
+    reports the slowdown: a request's latency over the plain path's median
+    latency for a request of its size (sizes span 2^14 to 2^26, so raw
+    latency percentiles mostly reflect the size mix).  The saturating point
+    (1.5 x) serves ``--serve-requests`` requests (10k by default); the lighter
+    loads a tenth of that."""
     import numpy as np
     from bitz_gb300 import serve as S
 
@@ -732,11 +782,24 @@ def _bench_serve(ctx, bz, args, plain_rate=None):
     hp = ctypes.c_void_p()
     _lib.check(None, L.bz_host_alloc_pinned(16 * max_n, ctypes.byref(hp)))
     _lib.check(None, L.bz_chacha_fill_host(4, 0, hp, max_n, os.cpu_count() or 1))
-    base = plain_rate or 4.0e9
-    out = {"requests_at_saturation": args.serve_requests, "unit": UNIT,
-           "sizes": "truncated geometric on [14,26], q=0.97", "load_reference": base,
-           "rates": []}
     params = {k: bz.PcsParams(k + 7, 2, k // 2, 1) for k in range(14, 27)}
+    # warm every shape once (twiddles, schedules), then the plain baseline
+    _bench_plain_mix(ctx, bz, L, _lib, hp, list(range(14, 27)), params)
+    plain_sizes = _geometric_sizes(np.random.default_rng(5), max(args.serve_requests // 5, 200))
+    plain, solo_ms = _bench_plain_mix(ctx, bz, L, _lib, hp, plain_sizes, params)
+    _, solo_all = _bench_plain_mix(ctx, bz, L, _lib, hp, list(range(14, 27)) * 3, params)
+    for k, v in solo_all.items():
+        solo_ms.setdefault(k, v)
+    base = plain
+    out = {"requests_at_saturation": args.serve_requests, "unit": UNIT,
+           "sizes": "truncated geometric on [14,26], q=0.97",
+           "plain_same_mix": plain,
+           "plain_same_mix_requests": len(plain_sizes),
+           "plain_same_mix_path": "one request at a time: bz_commit (host message, H2D inside) "
+                                  "+ bz_commitment_rows + bz_commitment_multiproof at 3 positions",
+           "load_reference": base, "c4_mix_plain_device_rate": plain_rate,
+           "solo_ms_by_log2_size": {str(k): v for k, v in sorted(solo_ms.items())},
+           "rates": []}
     for load in (0.3, 0.6, 0.9, 1.5):
         n_req = args.serve_requests if load >= 1.0 else max(args.serve_requests // 10, 50)
         sizes = _geometric_sizes(rng, n_req)
@@ -745,14 +808,16 @@ def _bench_serve(ctx, bz, args, plain_rate=None):
         arrivals = np.cumsum(rng.exponential(1.0 / lam, n_req))
         with S.Server(ctx, n_slots=4) as srv:
             srv.next_done(0, 0)                           # start the completion queue
-            lat = []
+            lat, slow = [], []
+            rid_size = {}
             t0 = time.perf_counter()
             i = done = 0
             while done < n_req:
                 now = time.perf_counter() - t0
                 while i < n_req and arrivals[i] <= now:
                     k = int(sizes[i])
-                    srv.submit_commit_open_ptr(hp.value, 1 << k, params[k], [0, 1, 7])
+                    rid = srv.submit_commit_open_ptr(hp.value, 1 << k, params[k], [0, 1, 7])
+                    rid_size[rid] = k
                     i += 1
                 if i < n_req:
                     wait_us = int(max(0.0, arrivals[i] - (time.perf_counter() - t0)) * 1e6)
@@ -761,17 +826,23 @@ def _bench_serve(ctx, bz, args, plain_rate=None):
                 for rid, st in srv.next_done(256, wait_us):
                     if st == S.OPENED:
                         t = srv.times(rid)
-                        lat.append((t[4] - t[0]) / 1e6)
+                        ms = (t[4] - t[0]) / 1e6
+                        lat.append(ms)
+                        slow.append(ms / solo_ms[rid_size.pop(rid)])
                         srv.release(rid)
                         done += 1
                     elif st == S.FAILED:
                         raise RuntimeError("serving request failed")
             wall = time.perf_counter() - t0
         lat.sort()
+        slow.sort()
+        q = lambda a, f: a[min(len(a) - 1, int(f * len(a)))]
         out["rates"].append({
             "offered_load": load, "requests": n_req, "log2_size_mean": float(sizes.mean()),
             "arrival_rate_per_s": lam, "throughput": total_elems / wall,
-            "p50_ms": lat[len(lat) // 2], "p99_ms": lat[min(len(lat) - 1, int(0.99 * len(lat)))],
+            "throughput_vs_plain_same_mix": total_elems / wall / plain,
+            "p50_ms": q(lat, 0.5), "p99_ms": q(lat, 0.99),
+            "slowdown_p50": q(slow, 0.5), "slowdown_p99": q(slow, 0.99),
             "wall_s": wall})
     L.bz_host_free_pinned(hp)
     return out

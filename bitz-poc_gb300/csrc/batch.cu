@@ -201,6 +201,11 @@ int bz_autotune(bz_ctx *ctx, const bz_params *params, int reps, uint32_t *chosen
     }
     std::vector<uint32_t> cands;
     const int b = s.log_dim();
+    if (s.log_lanes >= 9 && s.k_code() - s.log_inv_rate >= 3) {
+        // radix-8 passes, the leftover layers last or first
+        cands.push_back(SCHED_RADIX8);
+        if ((s.k_code() - s.log_inv_rate) % 3) cands.push_back(SCHED_RADIX8 | SCHED_R8_HEAD);
+    }
     for (int d = 0; d <= std::min(4, b); ++d) {
         for (uint32_t r2 : {0u, (uint32_t)SCHED_RADIX2}) {
             if (d == 0) {

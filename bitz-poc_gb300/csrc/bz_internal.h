@@ -64,6 +64,8 @@ enum : uint32_t {
     SCHED_PREFETCH = 0x1000,      // radix-4 table passes double-buffer their loads
     SCHED_LEAN = 0x2000,          // cap table-pass registers (room for co-resident CTAs)
     SCHED_NARROW = 0x4000,        // compact 32-bit tables for the deepest layers' twiddles
+    SCHED_RADIX8 = 0x8000,        // radix-8 passes (eight 32 KB byte tables per twiddle)
+    SCHED_R8_HEAD = 0x10000,      // with SCHED_RADIX8: the 1-2 leftover layers run first
 };
 uint32_t default_schedule(const Shape &s);
 

@@ -42,6 +42,7 @@
 #include "bz_internal.h"
 #include "gf128.cuh"
 #include "t16.cuh"
+#include "t8.cuh"
 
 namespace bz {
 
@@ -126,10 +127,12 @@ int twiddle_bits(int ell, int layer) {
 
 // Schedule of a shape the autotuner has not timed.  With at least 512 lanes
 // every layer fits the table passes (each 512-thread chunk stays inside one
-// block), and prefetching radix-4 passes with compact tables for the narrow
-// deep twiddles are what the autotuner picks at 2^20, 2^24 and 2^28; narrower
-// shapes run their last three layers in the register-resident deep pass.
+// block); radix-8 passes (three layers per sweep) measured faster than the
+// prefetching radix-4 passes at 2^20, 2^24 and 2^28 (3.33 against 3.49 ms at
+// 2^24); narrower shapes run their last three layers in the
+// register-resident deep pass.
 uint32_t default_schedule(const Shape &s) {
+    if (s.log_lanes >= 9 && s.k_code() - s.log_inv_rate >= 3) return SCHED_RADIX8;
     if (s.log_lanes >= 9) return SCHED_PREFETCH | SCHED_NARROW;
     const int layers = s.log_dim();
     const int deep = std::min(layers, 3);
@@ -277,24 +280,27 @@ constexpr int narrow_class(int bits) { return bits + 7 <= 32 ? 1 : (bits + 7 <= 
 // pair (x, h) writes half of x's copies, rotated by x, so that every store
 // instruction of a warp covers the banks once.
 template <int W>
-__device__ __forceinline__ void nw_build(char *tb, uint64_t t) {
+__device__ __forceinline__ void nw_build_item(char *tb, uint64_t t, int u) {
     constexpr int copies = W == 1 ? 32 : 16, half = copies / 2;
-    for (int u = threadIdx.x; u < 512; u += blockDim.x) {
-        const uint32_t x = (uint32_t)u >> 1, h = (uint32_t)u & 1;
-        uint64_t p = 0;
+    const uint32_t x = (uint32_t)u >> 1, h = (uint32_t)u & 1;
+    uint64_t p = 0;
 #pragma unroll
-        for (int i = 0; i < 8; ++i)
-            if ((x >> i) & 1) p ^= t << i;
+    for (int i = 0; i < 8; ++i)
+        if ((x >> i) & 1) p ^= t << i;
 #pragma unroll
-        for (int i = 0; i < half; ++i) {
-            const uint32_t c = h * half + ((i + x) & (half - 1));
-            if (W == 1)
-                reinterpret_cast<uint32_t *>(tb)[x * 32 + c] = (uint32_t)p;
-            else
-                reinterpret_cast<uint2 *>(tb)[x * 16 + c] =
-                    make_uint2((uint32_t)p, (uint32_t)(p >> 32));
-        }
+    for (int i = 0; i < half; ++i) {
+        const uint32_t c = h * half + ((i + x) & (half - 1));
+        if (W == 1)
+            reinterpret_cast<uint32_t *>(tb)[x * 32 + c] = (uint32_t)p;
+        else
+            reinterpret_cast<uint2 *>(tb)[x * 16 + c] =
+                make_uint2((uint32_t)p, (uint32_t)(p >> 32));
     }
+}
+
+template <int W>
+__device__ __forceinline__ void nw_build(char *tb, uint64_t t) {
+    for (int u = threadIdx.x; u < 512; u += blockDim.x) nw_build_item<W>(tb, t, u);
 }
 
 // t * v through the compact table tb of width W.
@@ -438,6 +444,142 @@ __global__ void __launch_bounds__(THREADS, MINB) ntt_table_pass2_pf(TablePassArg
 #pragma unroll
         for (int g = 0; g < 4; ++g) {
             const uint64_t p = (B << (log_q + 2)) + ((uint64_t)g << log_q) + rr;
+            __stcs(a.dst + ((p << a.log_lanes) | ln), v[g]);
+        }
+    }
+}
+
+// ---- Radix-8 passes ---------------------------------------------------------
+// Layers l, l+1, l+2 on octets at positions B*8Q + g*Q + rr (g = 0..7),
+// Q = 2^(ell - l - 3):
+//   layer l  : pairs (g, g+4), g < 4, with twiddle(l, B)
+//   layer l+1: (0,2), (1,3) with twiddle(l+1, 2B); (4,6), (5,7) with
+//              twiddle(l+1, 2B+1)
+//   layer l+2: (2j, 2j+1) with twiddle(l+2, 4B+j), j < 4
+// i.e. the three single layers of additive_ntt_f128.rs:243-274 applied in
+// order (u <- u + t*v; v <- v + u), twelve multiplies per octet.  The seven
+// twiddles of a block B multiply through 32 KB tables each (224 KB): eight
+// byte tables of 16-byte entries (t8.cuh, width 4) or, for a narrow twiddle,
+// the compact one- or two-word table (width 1 or 2).  One sweep over the
+// codeword does three layers where the 64 KB radix-4 tables allow two.
+constexpr int kTw8Window = 8;
+constexpr int kPass8Smem = 7 * kT8Bytes;
+
+__device__ __forceinline__ uint4 tw8_at(const uint4 *tw, int layer, uint64_t B, int j) {
+    if (j == 0) return tw[((uint64_t)1 << layer) + B];
+    if (j < 3) return tw[((uint64_t)1 << (layer + 1)) + 2 * B + (uint64_t)(j - 1)];
+    return tw[((uint64_t)1 << (layer + 2)) + 4 * B + (uint64_t)(j - 3)];
+}
+
+// Table-build work items per twiddle: 128 for the byte tables (t8_build_item),
+// 512 for a compact table (nw_build_item).
+template <int W>
+constexpr int build_items() { return W == 4 ? 128 : 512; }
+
+template <int W>
+__device__ __forceinline__ void build_item(char *tb, uint4 t, int u) {
+    if constexpr (W == 4) t8_build_item(tb, t, u);
+    else nw_build_item<W>(tb, (uint64_t)t.x | ((uint64_t)t.y << 32), u);
+}
+
+template <int W>
+__device__ __forceinline__ uint4 pass_mul(const T8Lane &lc, const char *tb, uint4 v) {
+    if constexpr (W == 4) return lc.mul(tb, v);
+    else return nw_mul<W>(tb, v);
+}
+
+template <int W0, int W1, int W2>
+__global__ void __launch_bounds__(512, 1) ntt_pass8(TablePassArgs a) {
+    extern __shared__ uint4 smem[];
+    char *tbl = reinterpret_cast<char *>(smem);
+    __shared__ uint4 tw_buf[kTw8Window * 7];
+    __shared__ uint64_t win[2];
+    if (threadIdx.x == 0) win[0] = win[1] = 0;
+    T8Lane lc;
+    lc.init();
+    const int log_q = a.ell - a.layer - 3;
+    const int log_task_per_b = log_q + a.log_lanes;
+    const uint64_t lanes_mask = ((uint64_t)1 << a.log_lanes) - 1;
+    const uint64_t q_mask = ((uint64_t)1 << log_q) - 1;
+    const uint64_t src_mask = ((uint64_t)1 << a.src_pos_bits) - 1;
+    const uint64_t chunks = a.n_tasks / blockDim.x;
+    const uint64_t c_beg = chunks * blockIdx.x / gridDim.x;
+    const uint64_t c_end = chunks * (blockIdx.x + 1) / gridDim.x;
+    const uint64_t b_last = (a.task_base + c_end * blockDim.x - 1) >> log_task_per_b;
+    int64_t cur_b = -1;
+    uint32_t zmask = 0;  // zero twiddles of the current block
+    constexpr int n0 = build_items<W0>(), n1 = build_items<W1>(), n2 = build_items<W2>();
+    constexpr int n_items = n0 + 2 * n1 + 4 * n2;
+    for (uint64_t c = c_beg; c < c_end; ++c) {
+        const uint64_t task = a.task_base + c * blockDim.x + threadIdx.x;
+        const uint64_t B = task >> log_task_per_b;  // uniform across the CTA
+        if ((int64_t)B != cur_b) {
+            __syncthreads();  // every lookup into the previous block's tables is done
+            uint64_t b0 = win[0];
+            if (B >= b0 + win[1]) {  // uniform: all threads read win[] after a barrier
+                const uint64_t n = min((uint64_t)kTw8Window, b_last + 1 - B);
+                for (uint64_t j = threadIdx.x; j < n * 7; j += blockDim.x)
+                    tw_buf[j] = tw8_at(a.tw, a.layer, B + j / 7, (int)(j % 7));
+                __syncthreads();
+                if (threadIdx.x == 0) {
+                    win[0] = B;
+                    win[1] = n;
+                }
+                b0 = B;
+            }
+            const uint4 *ts = tw_buf + (B - b0) * 7;
+            zmask = 0;
+#pragma unroll
+            for (int j = 0; j < 7; ++j) zmask |= gf_is_zero(ts[j]) ? (1u << j) : 0u;
+            for (int u = threadIdx.x; u < n_items; u += blockDim.x) {
+                if (u < n0) {
+                    build_item<W0>(tbl, ts[0], u);
+                } else if (u < n0 + 2 * n1) {
+                    const int k = (u - n0) / n1;
+                    build_item<W1>(tbl + (1 + k) * kT8Bytes, ts[1 + k], (u - n0) - k * n1);
+                } else {
+                    const int k = (u - n0 - 2 * n1) / n2;
+                    build_item<W2>(tbl + (3 + k) * kT8Bytes, ts[3 + k], (u - n0 - 2 * n1) - k * n2);
+                }
+            }
+            __syncthreads();
+            cur_b = (int64_t)B;
+        }
+        const uint64_t rr = (task >> a.log_lanes) & q_mask;
+        const uint64_t ln = task & lanes_mask;
+        const uint64_t pbase = (B << (log_q + 3)) + rr;
+        uint4 v[8];
+#pragma unroll
+        for (int g = 0; g < 8; ++g) {
+            const uint64_t p = pbase + ((uint64_t)g << log_q);
+            v[g] = __ldcs(a.src + (((p & src_mask) << a.log_lanes) | ln));
+        }
+        if (!(zmask & 1)) {
+#pragma unroll
+            for (int g = 0; g < 4; ++g) v[g] = gf_add(v[g], pass_mul<W0>(lc, tbl, v[g + 4]));
+        }
+#pragma unroll
+        for (int g = 0; g < 4; ++g) v[g + 4] = gf_add(v[g + 4], v[g]);
+#pragma unroll
+        for (int h = 0; h < 2; ++h) {
+            const char *tb = tbl + (1 + h) * kT8Bytes;
+            uint4 &x0 = v[4 * h], &x1 = v[4 * h + 1], &x2 = v[4 * h + 2], &x3 = v[4 * h + 3];
+            if (!(zmask & (2u << h))) {
+                x0 = gf_add(x0, pass_mul<W1>(lc, tb, x2));
+                x1 = gf_add(x1, pass_mul<W1>(lc, tb, x3));
+            }
+            x2 = gf_add(x2, x0);
+            x3 = gf_add(x3, x1);
+        }
+#pragma unroll
+        for (int j = 0; j < 4; ++j) {
+            const char *tb = tbl + (3 + j) * kT8Bytes;
+            if (!(zmask & (8u << j))) v[2 * j] = gf_add(v[2 * j], pass_mul<W2>(lc, tb, v[2 * j + 1]));
+            v[2 * j + 1] = gf_add(v[2 * j + 1], v[2 * j]);
+        }
+#pragma unroll
+        for (int g = 0; g < 8; ++g) {
+            const uint64_t p = pbase + ((uint64_t)g << log_q);
             __stcs(a.dst + ((p << a.log_lanes) | ln), v[g]);
         }
     }
@@ -715,6 +857,48 @@ void init_ntt_kernels() {
 #undef BZ_PF_ATTR
     BZ_TAIL_ATTR_M(1, 1); BZ_TAIL_ATTR_M(1, 2); BZ_TAIL_ATTR_M(1, 3);
     BZ_TAIL_ATTR_M(2, 1); BZ_TAIL_ATTR_M(2, 2);
+#define BZ_P8_ATTR(A, B, C)                                                                  \
+    cudaFuncSetAttribute(ntt_pass8<A, B, C>, cudaFuncAttributeMaxDynamicSharedMemorySize,     \
+                         kPass8Smem)
+    BZ_P8_ATTR(4, 4, 4); BZ_P8_ATTR(4, 4, 2); BZ_P8_ATTR(4, 4, 1); BZ_P8_ATTR(4, 2, 2);
+    BZ_P8_ATTR(4, 2, 1); BZ_P8_ATTR(4, 1, 1); BZ_P8_ATTR(2, 2, 2); BZ_P8_ATTR(2, 2, 1);
+    BZ_P8_ATTR(2, 1, 1); BZ_P8_ATTR(1, 1, 1);
+#undef BZ_P8_ATTR
+}
+
+// One radix-8 pass over layers layer .. layer+2 of every position.  The table
+// width of each layer follows its widest twiddle; a shallower layer never
+// takes a narrower table than a deeper one of the same pass.
+// Returns whether any of its layers multiplies through compact tables.
+static bool launch_pass8(const Shape &s, int layer, const uint4 *src, int src_bits, uint4 *dst,
+                         const uint4 *tw, cudaStream_t st, int num_sms) {
+    const int ell = s.k_code(), L = s.log_lanes;
+    TablePassArgs a;
+    a.src = src;
+    a.dst = dst;
+    a.tw = tw;
+    a.ell = ell;
+    a.layer = layer;
+    a.log_lanes = L;
+    a.src_pos_bits = src_bits;
+    a.task_base = 0;
+    a.n_tasks = (((uint64_t)1 << ell) >> 3) << L;
+    int w2 = narrow_class(twiddle_bits(ell, layer + 2));
+    int w1 = std::max(narrow_class(twiddle_bits(ell, layer + 1)), w2);
+    int w0 = std::max(narrow_class(twiddle_bits(ell, layer)), w1);
+    const unsigned grid =
+        (unsigned)std::max<uint64_t>(1, std::min<uint64_t>(num_sms, a.n_tasks / 512));
+    const int key = w0 * 100 + w1 * 10 + w2;
+#define BZ_P8_CASE(A, B, C) \
+    case A * 100 + B * 10 + C: ntt_pass8<A, B, C><<<grid, 512, kPass8Smem, st>>>(a); break
+    switch (key) {
+        BZ_P8_CASE(4, 4, 2); BZ_P8_CASE(4, 4, 1); BZ_P8_CASE(4, 2, 2); BZ_P8_CASE(4, 2, 1);
+        BZ_P8_CASE(4, 1, 1); BZ_P8_CASE(2, 2, 2); BZ_P8_CASE(2, 2, 1); BZ_P8_CASE(2, 1, 1);
+        BZ_P8_CASE(1, 1, 1);
+        default: ntt_pass8<4, 4, 4><<<grid, 512, kPass8Smem, st>>>(a); break;
+    }
+#undef BZ_P8_CASE
+    return w2 < 4;
 }
 
 template <int D>
@@ -843,6 +1027,44 @@ int launch_ntt(const Shape &s, uint32_t schedule, const uint4 *d_msg, uint4 *d_c
             src = d_cw;
             src_bits = 62;
         }
+        return launches;
+    }
+    if ((schedule & SCHED_RADIX8) && L >= 9 && ell - r >= 3) {
+        // radix-8 passes; the 1-2 layers left over run as one radix-4 or
+        // radix-2 table pass, last (deepest, narrowest twiddles) or first
+        const int total = ell - r, rest = total % 3;
+        const bool head = (schedule & SCHED_R8_HEAD) != 0;
+        const uint32_t pass_sched = SCHED_PREFETCH | SCHED_NARROW;
+        int layer = r;
+        auto small_pass = [&](int layers) {
+            launches += launch_table_pass(s, layer, layers, src, src_bits, d_cw, d_tw, 0, P, 512,
+                                          st, num_sms, pass_sched);
+            if (log) {
+                std::string n = layers == 2 ? "ntt_table_pass2" : "ntt_table_pass1";
+                if (src == d_msg) n += "_first";
+                if (narrow_table_pass(s, pass_sched, layer, layers, 512)) n += "_nw";
+                log->mark((n + "@" + std::to_string(layer)).c_str());
+            }
+            src = d_cw;
+            src_bits = 62;
+            layer += layers;
+        };
+        if (head && rest) small_pass(rest);
+        while (ell - layer >= 3) {
+            const bool nw = launch_pass8(s, layer, src, src_bits, d_cw, d_tw, st, num_sms);
+            ++launches;
+            if (log) {
+                // "<kernel>@<first layer>": the profile's reader counts the
+                // multiplies of each launch from its layer
+                std::string n = src == d_msg ? "ntt_pass8_first" : "ntt_pass8";
+                if (nw) n += "_nw";
+                log->mark((n + "@" + std::to_string(layer)).c_str());
+            }
+            src = d_cw;
+            src_bits = 62;
+            layer += 3;
+        }
+        if (layer < ell) small_pass(ell - layer);
         return launches;
     }
     int deep = (int)(schedule & SCHED_DEEP_MASK);
