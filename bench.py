@@ -46,6 +46,12 @@ WORKLOAD = {
     "l2": "inputs larger than L2: 256 MiB message, 1 GiB codeword per step",
 }
 MSG_BYTES = 16 << LOG_N
+CPU_PORT_SAMPLE = ("{what} by oracle/oracle.c on all host threads: a C restatement of the "
+                   "reference's commit with its parallel structure (top NTT layers fused in "
+                   "pairs, deep layers per cache-resident 2 MiB sub-group, persistent thread "
+                   "pool, PMULL multiplies on aarch64), not the reference's own Rust code "
+                   "(no Rust toolchain on either machine); its BLAKE3 is a portable scalar "
+                   "restatement, where the reference's crate hashes with NEON/AVX")
 ALG_BYTES_PER_WORD = 16 + (16 << LOG_INV_RATE)   # read message + write codeword
 SCHED_PIPE_BITS = 3 << 10                         # pipeline chunk count of a schedule
 # One GF(2^128) multiply by a block twiddle = 16 byte-table lookups of 16 B.
@@ -195,9 +201,12 @@ def _peaks():
 
 def cpu_baseline(n_threads: int, log_n: int = LOG_N):
     """The oracle commit (CPU restatement of the reference) on a full 2^24
-    commit with all host threads; elements per second.  Also times the
-    oracle's recursive Ligerito proof of that commitment with the opening
-    leg's configuration (its folds run on one thread)."""
+    commit with all host threads; elements per second.  With several threads
+    the oracle runs the reference's parallel structure (top NTT layers fused
+    in pairs, deep layers per cache-resident 2 MiB sub-group, a persistent
+    thread pool; PMULL multiplies on aarch64), not its per-layer form.  Also
+    times the oracle's recursive Ligerito proof of that commitment with the
+    opening leg's configuration (its folds run on one thread)."""
     from oracle import oracle as O
     from oracle.ligerito import LigeritoConfig, prove
     from oracle.transcript import Blake3Transcript, ZincChallenger
@@ -253,9 +262,8 @@ def run_reference(args, ws, rank):
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "u64 (GF(2^128))",
         "data": "synthetic", "config": dict(WORKLOAD, parallelism=f"replicas{ws}"),
         "cpu_baseline": {"value": value, "unit": UNIT, "cores": threads, "kind": "port",
-                         "sample": "full 2^24-element commit per step (CPU restatement of the "
-                                   "reference, all host threads); no Rust toolchain for the "
-                                   "reference's own rayon path"},
+                         "sample": CPU_PORT_SAMPLE.format(what="full 2^24-element commit per "
+                                                                   "step")},
         "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }
     print(json.dumps(line), flush=True)
@@ -441,6 +449,24 @@ def run_gpu(args, ws, rank, local):
                                    f"median sampled SM clock {mhz} MHz"}
         commit_ms = statistics.median(step_ms)
         commit_gbs = ALG_BYTES_PER_WORD * (1 << LOG_N) / (commit_ms / 1e3) / 1e9
+        # whole-commit DRAM traffic: every launch's ncu bytes per codeword byte
+        # (the small tree levels excepted), when all of them were captured
+        commit_traffic, missing = 0.0, []
+        for kern, (n_l, _) in agg.items():
+            if kern in NCU_TRAFFIC_PER_CW_BYTE:
+                commit_traffic += n_l * NCU_TRAFFIC_PER_CW_BYTE[kern][0] * cw_bytes
+            elif not kern.startswith("merkle_levels"):
+                missing.append(kern)
+        commit_traffic = None if missing else commit_traffic
+        # every table pass's lookups over the commit time: the shared-memory
+        # pipe bound of the whole NTT
+        all_lb = [b for v in lookup_bytes.values() for b in v]
+        commit_smem = None
+        if all_lb and None not in all_lb and smem and smem["peak"]:
+            ach = sum(all_lb) / (commit_ms / 1e3) / 1e9
+            commit_smem = {"lookup_bytes": sum(all_lb), "achieved": ach, "peak": smem["peak"],
+                           "unit": "GB/s", "frac": ach / smem["peak"],
+                           "note": "wide-twiddle passes only; compact-table passes not counted"}
 
         # ---- batched (64 polys, log2 sizes U[16, 24], seed 3) vs plain -----
         batch = None
@@ -464,8 +490,8 @@ def run_gpu(args, ws, rank, local):
             v, dt, croot, cpu_open_ms, cpu_bit_mle_ms = cpu_baseline(threads)
             assert croot == root0 or rank != 0 or SEED + rank != SEED
             cpu = {"value": v, "unit": UNIT, "cores": threads, "kind": "port",
-                   "sample": f"one full 2^24-element commit ({dt:.2f} s) by the CPU "
-                             "restatement of the reference on all host threads",
+                   "sample": CPU_PORT_SAMPLE.format(
+                       what=f"one full 2^24-element commit ({dt:.2f} s)"),
                    "prove_ms": cpu_open_ms, "bit_mle_2^20_round0_and_open_ms": cpu_bit_mle_ms}
         sorted_ms = sorted(step_ms)
         p99 = sorted_ms[min(len(sorted_ms) - 1, int(round(0.99 * (len(sorted_ms) - 1))))]
@@ -482,14 +508,23 @@ def run_gpu(args, ws, rank, local):
                     "d2h_bytes_per_step": 32, "api": "bz_commit_async + bz_commitment_root",
                     "pipelined": "upload of step i+1 overlaps the kernels of step i",
                     "sync_call_value": ws * args.steps * (1 << LOG_N) / (e2e_sync_ms / 1e3)},
-            "roofline": {"bound": "hbm", "kernel": dom_name, "achieved": achieved, "peak": peak,
-                         "unit": "GB/s", "frac": achieved / peak, "traffic": traffic,
-                         "traffic_source": (NCU_TRAFFIC_PER_CW_BYTE[dom_name][1]
-                                            if traffic is not None else None),
-                         "alg_bytes_per_launch": alg_bytes, "launch_ms": dom_ms / dom_n,
-                         "peak_source": peak_kind, "phase_schedule": prof_schedule,
-                         "commit_alg_gbs": commit_gbs, "commit_frac": commit_gbs / peak,
-                         "smem": smem},
+            "roofline": {"bound": "hbm", "scope": "whole commit: 80 B per element (read "
+                                                    "the message, write the codeword) over "
+                                                    "the median commit time",
+                         "achieved": commit_gbs, "peak": peak, "unit": "GB/s",
+                         "frac": commit_gbs / peak, "traffic": commit_traffic,
+                         "traffic_source": ("ncu DRAM bytes of every launch, "
+                                            "profiles/traffic_commit_2e24.md"
+                                            if commit_traffic is not None else None),
+                         "peak_source": peak_kind, "smem_commit": commit_smem,
+                         "kernel": {"name": dom_name, "launches": dom_n,
+                                    "achieved": achieved, "peak": peak, "unit": "GB/s",
+                                    "frac": achieved / peak, "traffic": traffic,
+                                    "traffic_source": (NCU_TRAFFIC_PER_CW_BYTE[dom_name][1]
+                                                       if traffic is not None else None),
+                                    "alg_bytes_per_launch": alg_bytes,
+                                    "launch_ms": dom_ms / dom_n, "smem": smem},
+                         "phase_schedule": prof_schedule},
             "phases_ms": {k: round(v[1], 4) for k, v in agg.items()},
             "phase_share": {k: round(v[1] / total_phase, 4) for k, v in agg.items()},
             "clocks": clk, "gpu_launches": launches, "wall_s": wall,

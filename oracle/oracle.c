@@ -10,6 +10,8 @@
 #include "oracle.h"
 
 #include <pthread.h>
+#include <stdint.h>
+#include <stdatomic.h>
 #include <stdlib.h>
 #include <string.h>
 
@@ -324,6 +326,187 @@ void orc_ntt_forward_interleaved(uint64_t *data, size_t num_ntts, int log_d, int
             parallel_for(nblocks, n_threads, ntt_layer_blocks, &c);
         }
     }
+    free(ev);
+}
+
+/* ------------------------------------------------------------------------
+ * The same transform with the reference's parallel structure
+ * (forward_transform_interleaved_parallel_from_layer, :298-517): the top
+ * layers sweep the whole buffer two at a time (the fused 2-layer row op of
+ * :829-857, which is the two layers applied in order), and the deep layers
+ * run sub-group by sub-group, each sub-group (a block of at most 2 MiB) held
+ * in cache while all of its remaining layers are applied (:434-516).  Work is
+ * handed to a persistent pool of threads instead of threads started per
+ * layer.  Identical output to orc_ntt_forward_interleaved.
+ * ------------------------------------------------------------------------ */
+static struct {
+    pthread_mutex_t mu;
+    pthread_cond_t cv_work, cv_done;
+    int n_workers;
+    pthread_t th[256];
+    unsigned gen;
+    int pending;
+    range_fn fn;
+    void *ctx;
+    size_t n, chunk;
+    atomic_size_t next;
+} g_pool = {PTHREAD_MUTEX_INITIALIZER, PTHREAD_COND_INITIALIZER, PTHREAD_COND_INITIALIZER};
+
+static void pool_drain(void) {
+    for (;;) {
+        size_t i = atomic_fetch_add(&g_pool.next, g_pool.chunk);
+        if (i >= g_pool.n) break;
+        size_t hi = i + g_pool.chunk < g_pool.n ? i + g_pool.chunk : g_pool.n;
+        g_pool.fn(g_pool.ctx, i, hi);
+    }
+}
+
+/* arg: the generation current when the worker was created (before the job
+ * that created it was published), so that job is the first one it runs */
+static void *pool_worker(void *arg) {
+    unsigned seen = (unsigned)(uintptr_t)arg;
+    pthread_mutex_lock(&g_pool.mu);
+    for (;;) {
+        while (g_pool.gen == seen) pthread_cond_wait(&g_pool.cv_work, &g_pool.mu);
+        seen = g_pool.gen;
+        pthread_mutex_unlock(&g_pool.mu);
+        pool_drain();
+        pthread_mutex_lock(&g_pool.mu);
+        if (--g_pool.pending == 0) pthread_cond_signal(&g_pool.cv_done);
+    }
+    return NULL;
+}
+
+/* fn over [0, n) in chunks of `chunk` items, by the calling thread and up to
+ * n_threads - 1 pool workers (created once, kept for the process). */
+static void pool_run(size_t n, size_t chunk, int n_threads, range_fn fn, void *ctx) {
+    if (n_threads <= 1 || n <= chunk) {
+        fn(ctx, 0, n);
+        return;
+    }
+    if (n_threads > 256) n_threads = 256;
+    pthread_mutex_lock(&g_pool.mu);
+    while (g_pool.n_workers < n_threads - 1) {
+        if (pthread_create(&g_pool.th[g_pool.n_workers], NULL, pool_worker,
+                           (void *)(uintptr_t)g_pool.gen) != 0)
+            break;
+        g_pool.n_workers++;
+    }
+    g_pool.fn = fn;
+    g_pool.ctx = ctx;
+    g_pool.n = n;
+    g_pool.chunk = chunk ? chunk : 1;
+    atomic_store(&g_pool.next, 0);
+    g_pool.pending = g_pool.n_workers;
+    g_pool.gen++;
+    pthread_cond_broadcast(&g_pool.cv_work);
+    pthread_mutex_unlock(&g_pool.mu);
+    pool_drain();
+    pthread_mutex_lock(&g_pool.mu);
+    while (g_pool.pending > 0) pthread_cond_wait(&g_pool.cv_done, &g_pool.mu);
+    pthread_mutex_unlock(&g_pool.mu);
+}
+
+/* u <- u + t v ; v <- v + u over `lanes` lanes of rows u and v */
+static inline void butterfly_rows(uint64_t *u, uint64_t *v, size_t lanes, const uint64_t t[2]) {
+    const int zero = (t[0] | t[1]) == 0;
+    for (size_t lane = 0; lane < lanes; ++lane) {
+        uint64_t *a = u + 2 * lane, *b = v + 2 * lane;
+        if (!zero) {
+            uint64_t p[2];
+            gf_mul(b, t, p);
+            a[0] ^= p[0];
+            a[1] ^= p[1];
+        }
+        b[0] ^= a[0];
+        b[1] ^= a[1];
+    }
+}
+
+struct ntt_blk_ctx {
+    uint64_t *data;
+    const uint64_t *evals;
+    size_t lanes;
+    int l, layer, deep_start;
+};
+
+/* Fused pair of top layers (layer, layer+1): item = (block B, row rr) of the
+ * quads at positions B*4Q + g*Q + rr, g = 0..3. */
+static void ntt_pair_items(void *p, size_t lo, size_t hi) {
+    struct ntt_blk_ctx *c = (struct ntt_blk_ctx *)p;
+    const int log_q = c->l - c->layer - 2;
+    const size_t Q = (size_t)1 << log_q, row = 2 * c->lanes;
+    for (size_t it = lo; it < hi; ++it) {
+        const size_t B = it >> log_q, rr = it & (Q - 1);
+        uint64_t to[2], ta[2], tb[2];
+        twiddle_from_evals(c->evals, c->l, c->layer, B, to);
+        twiddle_from_evals(c->evals, c->l, c->layer + 1, 2 * B, ta);
+        twiddle_from_evals(c->evals, c->l, c->layer + 1, 2 * B + 1, tb);
+        uint64_t *x0 = c->data + (B * 4 * Q + rr) * row;
+        uint64_t *x1 = x0 + Q * row, *x2 = x1 + Q * row, *x3 = x2 + Q * row;
+        butterfly_rows(x0, x2, c->lanes, to);
+        butterfly_rows(x1, x3, c->lanes, to);
+        butterfly_rows(x0, x1, c->lanes, ta);
+        butterfly_rows(x2, x3, c->lanes, tb);
+    }
+}
+
+/* A single top layer: item = (block B, row rr) of the pair (rr, rr + half). */
+static void ntt_single_items(void *p, size_t lo, size_t hi) {
+    struct ntt_blk_ctx *c = (struct ntt_blk_ctx *)p;
+    const int log_h = c->l - c->layer - 1;
+    const size_t H = (size_t)1 << log_h, row = 2 * c->lanes;
+    for (size_t it = lo; it < hi; ++it) {
+        const size_t B = it >> log_h, rr = it & (H - 1);
+        uint64_t t[2];
+        twiddle_from_evals(c->evals, c->l, c->layer, B, t);
+        uint64_t *u = c->data + (B * 2 * H + rr) * row;
+        butterfly_rows(u, u + H * row, c->lanes, t);
+    }
+}
+
+/* Deep layers of one cache-resident sub-group: item = sub-group index G (the
+ * block of layer deep_start), every layer from deep_start down to the last. */
+static void ntt_subgroup_items(void *p, size_t lo, size_t hi) {
+    struct ntt_blk_ctx *c = (struct ntt_blk_ctx *)p;
+    const size_t row = 2 * c->lanes;
+    for (size_t G = lo; G < hi; ++G) {
+        for (int layer = c->deep_start; layer < c->l; ++layer) {
+            const int d = layer - c->deep_start;          /* sub-blocks of G at this layer */
+            const size_t H = (size_t)1 << (c->l - layer - 1);
+            for (size_t sb = 0; sb < ((size_t)1 << d); ++sb) {
+                const size_t B = (G << d) | sb;
+                uint64_t t[2];
+                twiddle_from_evals(c->evals, c->l, layer, B, t);
+                uint64_t *base = c->data + B * 2 * H * row;
+                for (size_t rr = 0; rr < H; ++rr)
+                    butterfly_rows(base + rr * row, base + (rr + H) * row, c->lanes, t);
+            }
+        }
+    }
+}
+
+void orc_ntt_forward_interleaved_blocked(uint64_t *data, size_t num_ntts, int log_d,
+                                         int start_layer, int n_threads) {
+    if (log_d <= 0 || start_layer >= log_d) return;
+    uint64_t *ev = (uint64_t *)malloc(sizeof(uint64_t) * 2 * (size_t)log_d * log_d);
+    orc_ntt_evals(log_d, ev);
+    /* sub-groups of 2^s positions, at most 2 MiB (at least one pair) */
+    int s = 1;
+    while (s < log_d - start_layer && ((size_t)2 << s) * num_ntts * 16 <= ((size_t)2 << 20)) ++s;
+    struct ntt_blk_ctx c = {data, ev, num_ntts, log_d, start_layer, log_d - s};
+    int layer = start_layer;
+    while (layer < c.deep_start) {
+        c.layer = layer;
+        if (layer + 1 < c.deep_start) {
+            pool_run((size_t)1 << (log_d - 2), 16, n_threads, ntt_pair_items, &c);
+            layer += 2;
+        } else {
+            pool_run((size_t)1 << (log_d - 1), 16, n_threads, ntt_single_items, &c);
+            layer += 1;
+        }
+    }
+    pool_run((size_t)1 << c.deep_start, 1, n_threads, ntt_subgroup_items, &c);
     free(ev);
 }
 
@@ -790,8 +973,12 @@ int orc_commit(const uint64_t *msg, int log_msg_len, int log_inv_rate, int log_b
     /* replicate_message_fill (:239-258): 2^r copies == state after r layers */
     for (size_t r = 0; r < reps; ++r)
         memcpy(codeword + 2 * r * msg_len, msg, sizeof(uint64_t) * 2 * msg_len);
-    /* finalize_commit (:262-315): NTT from layer r, Merkle over positions */
-    orc_ntt_forward_interleaved(codeword, num_ntts, k_code, log_inv_rate, n_threads);
+    /* finalize_commit (:262-315): NTT from layer r, Merkle over positions;
+     * several threads run the reference's blocked structure */
+    if (n_threads > 1)
+        orc_ntt_forward_interleaved_blocked(codeword, num_ntts, k_code, log_inv_rate, n_threads);
+    else
+        orc_ntt_forward_interleaved(codeword, num_ntts, k_code, log_inv_rate, 1);
     size_t n_leaves = (size_t)1 << k_code;
     orc_merkle_tree((const uint8_t *)codeword, 16 * msg_len * reps, n_leaves, hash_kind, tree,
                     n_threads);

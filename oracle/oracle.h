@@ -49,6 +49,10 @@ void orc_ntt_evals(int log_domain, uint64_t *out);
 void orc_ntt_forward_interleaved(uint64_t *data, size_t num_ntts, int log_d,
                                  int start_layer, int n_threads);
 /* single-lane forward transform (log_d layers) */
+/* the same transform, top layers fused in pairs, deep layers per cache-resident
+ * sub-group, on a persistent thread pool (the reference's parallel path) */
+void orc_ntt_forward_interleaved_blocked(uint64_t *data, size_t num_ntts, int log_d,
+                                         int start_layer, int n_threads);
 void orc_ntt_forward(uint64_t *data, int log_d);
 
 /* ---- hashes ---- */

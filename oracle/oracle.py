@@ -57,6 +57,7 @@ def _declare(L):
         "orc_ntt_evals": (None, [_I, _P]),
         "orc_ntt_forward_interleaved": (None, [_P, _S, _I, _I, _I]),
         "orc_ntt_forward": (None, [_P, _I]),
+        "orc_ntt_forward_interleaved_blocked": (None, [_P, _S, _I, _I, _I]),
         "orc_sha256": (None, [_P, _S, _P]),
         "orc_blake3_hash": (None, [_P, _S, _P]),
         "orc_blake3_xof": (None, [_P, _S, _P, _S]),
@@ -161,6 +162,14 @@ def ntt_forward_interleaved(data: np.ndarray, num_ntts: int, start_layer: int = 
     d = np.ascontiguousarray(data, np.uint64).copy()
     log_d = (d.shape[0] // num_ntts).bit_length() - 1
     lib().orc_ntt_forward_interleaved(_p(d), num_ntts, log_d, start_layer, n_threads)
+    return d
+
+
+def ntt_forward_interleaved_blocked(data: np.ndarray, num_ntts: int, start_layer: int = 0,
+                                    n_threads: int = 1) -> np.ndarray:
+    d = np.ascontiguousarray(data, np.uint64).copy()
+    log_d = (d.shape[0] // num_ntts).bit_length() - 1
+    lib().orc_ntt_forward_interleaved_blocked(_p(d), num_ntts, log_d, start_layer, n_threads)
     return d
 
 

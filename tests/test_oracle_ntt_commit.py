@@ -131,3 +131,18 @@ def test_roots_fixture_small(oracle):
         kind = 1 if e["hash"] == "blake3" else 0
         _, _, root = oracle.commit(z, e["log_inv_rate"], e["log_batch_size"], kind, 4)
         assert root.hex() == e["root"], e
+
+
+@pytest.mark.parametrize("ld,lanes,start,threads", [(6, 1, 0, 1), (8, 4, 2, 4), (12, 64, 2, 8),
+                                                    (10, 512, 1, 3), (14, 128, 2, 16),
+                                                    (16, 32, 3, 8), (9, 4096, 2, 8)])
+def test_blocked_parallel_ntt_equals_per_layer(ld, lanes, start, threads):
+    """The oracle's parallel form (top layers fused in pairs, deep layers per
+    cache-resident sub-group, persistent thread pool: the structure of the
+    reference's parallel path) equals the per-layer scalar form."""
+    from oracle import oracle as O
+
+    d = O.chacha_words(ld * 7 + lanes, lanes << ld)
+    a = O.ntt_forward_interleaved(d, lanes, start, 1)
+    b = O.ntt_forward_interleaved_blocked(d, lanes, start, threads)
+    assert (a == b).all()
