@@ -304,40 +304,60 @@ __device__ __forceinline__ void nw_build(char *tb, uint64_t t) {
 }
 
 // t * v through the compact table tb of width W.
+//
+// The lookups of byte position r of the four operand words are gathered
+// unshifted into one multi-word value S_r = XOR_q u[byte r of word q] << 32q
+// (for W = 1 every word of S_r is a single lookup, for W = 2 neighbouring
+// entries overlap by one word), and t * v = reduce(XOR_r S_r << 8r): one
+// funnel shift per word and byte position instead of two shifts and two
+// xors per lookup, which keeps this ALU-bound multiply off the ALU pipe.
 template <int W>
 __device__ __forceinline__ uint4 nw_mul(const char *tb, uint4 v) {
     const uint32_t lane_off = W == 1 ? (threadIdx.x & 31) << 2 : (threadIdx.x & 15) << 3;
     const uint32_t w[4] = {v.x, v.y, v.z, v.w};
-    uint32_t acc[6] = {0, 0, 0, 0, 0, 0};
+    constexpr int NS = W == 1 ? 4 : 5;  // words of S_r
+    uint32_t S[4][NS];
 #pragma unroll
-    for (int q = 0; q < 4; ++q) {
+    for (int r = 0; r < 4; ++r) {
 #pragma unroll
-        for (int r = 0; r < 4; ++r) {
+        for (int q = 0; q < 4; ++q) {
             // byte r of word q, times 128 (the row pitch of both layouts)
             const uint32_t x7 = (r == 0 ? (w[q] << 7) : (w[q] >> (8 * r - 7))) & 0x7F80u;
-            if (W == 1) {
-                const uint32_t u = *reinterpret_cast<const uint32_t *>(tb + (x7 | lane_off));
-                acc[q] ^= u << (8 * r);
-                if (r) acc[q + 1] ^= u >> (32 - 8 * r);
+            if constexpr (W == 1) {
+                S[r][q] = *reinterpret_cast<const uint32_t *>(tb + (x7 | lane_off));
             } else {
                 const uint2 u = *reinterpret_cast<const uint2 *>(tb + (x7 | lane_off));
-                if (r == 0) {
-                    acc[q] ^= u.x;
-                    acc[q + 1] ^= u.y;
-                } else {
-                    acc[q] ^= u.x << (8 * r);
-                    acc[q + 1] ^= __funnelshift_l(u.x, u.y, 8 * r);
-                    acc[q + 2] ^= u.y >> (32 - 8 * r);
-                }
+                if (q == 0) S[r][0] = u.x;
+                else S[r][q] ^= u.x;
+                S[r][q + 1] = u.y;
             }
         }
     }
-    // bits 128 and up: X^128 = X^7 + X^2 + X + 1
-    const uint64_t h = (uint64_t)acc[4] | ((uint64_t)acc[5] << 32);
-    const uint64_t f = h ^ (h << 1) ^ (h << 2) ^ (h << 7);
-    // h < 2^56 (products of at most 64 bits shifted by at most 120), so f
-    // stays below 2^63 and needs no second fold
-    return make_uint4(acc[0] ^ (uint32_t)f, acc[1] ^ (uint32_t)(f >> 32), acc[2], acc[3]);
+    // acc = XOR_r S_r << 8r (NS + 1 words)
+    uint32_t acc[6];
+#pragma unroll
+    for (int k = 0; k <= NS; ++k) {
+        uint32_t x = k < NS ? S[0][k] : 0u;
+#pragma unroll
+        for (int r = 1; r < 4; ++r) {
+            const uint32_t hi = k < NS ? S[r][k] : 0u, lo = k > 0 ? S[r][k - 1] : 0u;
+            x ^= __funnelshift_l(lo, hi, 8 * r);
+        }
+        acc[k] = x;
+    }
+    // bits 128 and up: X^128 = X^7 + X^2 + X + 1.  W = 1: the products have
+    // at most 32 bits, so bits 128+ are below 2^24 and the fold stays in one
+    // word; W = 2: at most 64-bit products, h < 2^56 and f stays below 2^63,
+    // so neither needs a second fold.
+    if constexpr (W == 1) {
+        const uint32_t h = acc[4];
+        const uint32_t f = h ^ (h << 1) ^ (h << 2) ^ (h << 7);
+        return make_uint4(acc[0] ^ f, acc[1], acc[2], acc[3]);
+    } else {
+        const uint64_t h = (uint64_t)acc[4] | ((uint64_t)acc[5] << 32);
+        const uint64_t f = h ^ (h << 1) ^ (h << 2) ^ (h << 7);
+        return make_uint4(acc[0] ^ (uint32_t)f, acc[1] ^ (uint32_t)(f >> 32), acc[2], acc[3]);
+    }
 }
 
 // Radix-4 table pass with the next task's four loads issued before the
