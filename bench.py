@@ -61,9 +61,15 @@ SMEM_BYTES_PER_CLK_PER_SM = 128
 # captures of the same kernels on GB300 (dram__bytes_read.sum +
 # dram__bytes_write.sum), with the profile they come from.
 NCU_TRAFFIC_PER_CW_BYTE = {
-    "ntt_table_pass2": (1.940, "profiles/traffic_commit_2e24.md (mean of the 5 in-place passes)"),
-    "ntt_table_pass2_first": (1.427, "profiles/traffic_commit_2e24.md"),
-    "b3_leaves_chunked": (1.073, "profiles/traffic_commit_2e24.md"),
+    "ntt_pass8_first": (1.424, "profiles/launches_commit_2e24.md"),
+    "ntt_pass8": (1.941, "profiles/launches_commit_2e24.md (both in-place byte-table passes)"),
+    "ntt_pass8_nw": (1.940, "profiles/launches_commit_2e24.md"),
+    "b3_leaves_chunked": (1.057, "profiles/launches_commit_2e24.md"),
+    # radix-4 schedules sweep the codeword the same way: one read and one
+    # write in place, the first pass reading the message instead
+    "ntt_table_pass2_first": (1.424, "profiles/launches_commit_2e24.md (a first sweep)"),
+    "ntt_table_pass2": (1.941, "profiles/launches_commit_2e24.md (an in-place sweep)"),
+    "ntt_table_pass2_nw": (1.940, "profiles/launches_commit_2e24.md (an in-place sweep)"),
 }
 
 
@@ -514,7 +520,7 @@ def run_gpu(args, ws, rank, local):
                          "achieved": commit_gbs, "peak": peak, "unit": "GB/s",
                          "frac": commit_gbs / peak, "traffic": commit_traffic,
                          "traffic_source": ("ncu DRAM bytes of every launch, "
-                                            "profiles/traffic_commit_2e24.md"
+                                            "profiles/launches_commit_2e24.md"
                                             if commit_traffic is not None else None),
                          "peak_source": peak_kind, "smem_commit": commit_smem,
                          "kernel": {"name": dom_name, "launches": dom_n,
