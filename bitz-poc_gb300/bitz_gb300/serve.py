@@ -4,7 +4,9 @@
 scheduler admits it when an execution slot and device memory are free.
 ``submit_open`` queues the opening (rows + multi-proof) of a committed
 request, after which its resident codeword and tree are freed;
-``submit_commit_open`` queues both at once.  ``next_done`` is the completion
+``submit_commit_open`` runs both back to back on one stream.  Queued commits
+are admitted smallest first (a request that waited past the aging bound goes
+first), small requests on high-priority streams (``set_policy``).  ``next_done`` is the completion
 queue: the ids of requests whose state changed, without polling each one.
 """
 from __future__ import annotations
@@ -17,6 +19,7 @@ from ._lib import Params, check, lib, ptr
 from .pcs import Context, PcsParams, default_context
 
 QUEUED, RUNNING, COMMITTED, OPEN_QUEUED, OPENING, OPENED, FAILED = range(7)
+ADMIT_FIFO, ADMIT_SMALLEST = 0, 1
 
 _P = ctypes.c_void_p
 _S = ctypes.c_size_t
@@ -39,6 +42,7 @@ _SIGS = {
     "bz_server_release": (ctypes.c_int, [_P, _U64]),
     "bz_server_stats": (ctypes.c_int, [_P] + [ctypes.POINTER(_U64)] * 5),
     "bz_server_destroy": (ctypes.c_int, [_P]),
+    "bz_server_set_policy": (ctypes.c_int, [_P, ctypes.c_int, ctypes.c_uint32, ctypes.c_int]),
 }
 
 
@@ -70,6 +74,14 @@ class Server:
             self.h = None
 
     release = close
+
+    def set_policy(self, admit_order: int = ADMIT_SMALLEST, aging_ms: int = 500,
+                   high_priority_log_size: int = 20) -> None:
+        """Admission order (smallest first with an aging bound, or arrival
+        order) and the largest request (log2 elements) that runs on
+        high-priority streams (-1: none)."""
+        check(self.ctx.handle, self.L.bz_server_set_policy(self.h, admit_order, aging_ms,
+                                                           high_priority_log_size))
 
     def __enter__(self):
         return self

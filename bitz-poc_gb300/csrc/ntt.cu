@@ -139,6 +139,11 @@ uint32_t default_schedule(const Shape &s) {
     return (uint32_t)deep;
 }
 
+// CTAs per SM a table pass is cut into: 1 (one long CTA per SM) or, under
+// SCHED_SHORT_CTAS, 8 shorter ones, so a kernel of a higher-priority stream
+// waits for one of those instead of the whole pass to get an SM.
+static int cta_waves(uint32_t schedule) { return (schedule & SCHED_SHORT_CTAS) ? 8 : 1; }
+
 struct TablePassArgs {
     const uint4 *src;   // message (first pass) or codeword
     uint4 *dst;         // codeword
@@ -891,7 +896,7 @@ void init_ntt_kernels() {
 // takes a narrower table than a deeper one of the same pass.
 // Returns whether any of its layers multiplies through compact tables.
 static bool launch_pass8(const Shape &s, int layer, const uint4 *src, int src_bits, uint4 *dst,
-                         const uint4 *tw, cudaStream_t st, int num_sms) {
+                         const uint4 *tw, cudaStream_t st, int num_sms, int waves = 1) {
     const int ell = s.k_code(), L = s.log_lanes;
     TablePassArgs a;
     a.src = src;
@@ -907,7 +912,8 @@ static bool launch_pass8(const Shape &s, int layer, const uint4 *src, int src_bi
     int w1 = std::max(narrow_class(twiddle_bits(ell, layer + 1)), w2);
     int w0 = std::max(narrow_class(twiddle_bits(ell, layer)), w1);
     const unsigned grid =
-        (unsigned)std::max<uint64_t>(1, std::min<uint64_t>(num_sms, a.n_tasks / 512));
+        (unsigned)std::max<uint64_t>(1, std::min<uint64_t>((uint64_t)num_sms * waves,
+                                                           a.n_tasks / 512));
     const int key = w0 * 100 + w1 * 10 + w2;
 #define BZ_P8_CASE(A, B, C) \
     case A * 100 + B * 10 + C: ntt_pass8<A, B, C><<<grid, 512, kPass8Smem, st>>>(a); break
@@ -963,7 +969,8 @@ int launch_table_pass(const Shape &s, int layer, int layers, const uint4 *src, i
     a.task_base = (b0 << log_q) << L;
     a.n_tasks = ((b1 - b0) << log_q) << L;
     const unsigned grid =
-        (unsigned)std::max<uint64_t>(1, std::min<uint64_t>(num_sms, a.n_tasks / threads));
+        (unsigned)std::max<uint64_t>(1, std::min<uint64_t>((uint64_t)num_sms * cta_waves(schedule),
+                                                           a.n_tasks / threads));
     if (narrow_table_pass(s, schedule, layer, layers, threads)) {
         const int wo = narrow_class(twiddle_bits(ell, layer));
         const int wab = narrow_class(twiddle_bits(ell, layer + 1));
@@ -1054,7 +1061,7 @@ int launch_ntt(const Shape &s, uint32_t schedule, const uint4 *d_msg, uint4 *d_c
         // radix-2 table pass, last (deepest, narrowest twiddles) or first
         const int total = ell - r, rest = total % 3;
         const bool head = (schedule & SCHED_R8_HEAD) != 0;
-        const uint32_t pass_sched = SCHED_PREFETCH | SCHED_NARROW;
+        const uint32_t pass_sched = SCHED_PREFETCH | SCHED_NARROW | (schedule & SCHED_SHORT_CTAS);
         int layer = r;
         auto small_pass = [&](int layers) {
             launches += launch_table_pass(s, layer, layers, src, src_bits, d_cw, d_tw, 0, P, 512,
@@ -1071,7 +1078,8 @@ int launch_ntt(const Shape &s, uint32_t schedule, const uint4 *d_msg, uint4 *d_c
         };
         if (head && rest) small_pass(rest);
         while (ell - layer >= 3) {
-            const bool nw = launch_pass8(s, layer, src, src_bits, d_cw, d_tw, st, num_sms);
+            const bool nw = launch_pass8(s, layer, src, src_bits, d_cw, d_tw, st, num_sms,
+                                         cta_waves(schedule));
             ++launches;
             if (log) {
                 // "<kernel>@<first layer>": the profile's reader counts the

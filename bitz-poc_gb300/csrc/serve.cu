@@ -15,8 +15,22 @@
 // to 256 BLAKE3 chunks); while it runs, the owning context may still be used
 // from other threads for unrelated work on the context stream.
 //
+// Scheduling: queued commits are admitted smallest first, except that a
+// request that has waited longer than the aging bound goes first (so a large
+// request is never starved), or in arrival order (bz_server_set_policy).
+// Half the slots run high-priority streams and take requests of at most 2^20
+// elements (and openings); large requests take the other half, whose table
+// passes run as short CTAs, so a small request's kernels get SMs within a
+// fraction of a large commit's pass.  A small request's message is read from
+// pinned host memory by a copy kernel, so it never queues behind a large
+// upload on the copy engine.  A commit-then-open
+// request enqueues its opening (row gather, multi-proof nodes, the copies to
+// the slot's pinned staging) right behind its commit on the same stream: one
+// completion, no second trip through the scheduler.  Each slot's work ends
+// with a host callback that wakes the scheduler.
+//
 // Nothing on the request path synchronises the device: device buffers come
-// from the stream-ordered pool (cudaMallocAsync / cudaFreeAsync on the slot's
+// from the server's stream-ordered pool (cudaMallocFromPoolAsync / cudaFreeAsync on the slot's
 // stream), and each slot owns its completion event and a grow-only pinned
 // staging buffer for the root, rows and proof nodes, which the scheduler
 // copies into the request when the slot's work completes.  A completion
@@ -28,7 +42,9 @@
 #include <condition_variable>
 #include <cstring>
 #include <algorithm>
+#include <atomic>
 #include <deque>
+#include <set>
 #include <map>
 #include <memory>
 #include <mutex>
@@ -65,7 +81,8 @@ struct Request {
     int slot = -1;
     uint8_t root[32] = {0};
     // opening
-    bool auto_open = false;  // queue the opening as soon as the commit is done
+    bool auto_open = false;  // open as soon as the commit is done
+    bool fused_open = false; // the opening was enqueued behind the commit
     std::vector<uint64_t> positions;
     std::vector<uint64_t> node_idx;
     std::vector<uint64_t> rows;  // q rows of 2^log_lanes elements
@@ -82,7 +99,13 @@ struct bz_server {
     int n_slots = 0;
     uint64_t budget = 0, in_use = 0;
     size_t queue_cap = 0;
+    // one stream per slot: the first n_hi slots have high priority and serve
+    // small requests (and openings), the others serve large ones (and small
+    // ones when every high slot is busy).  One stream per slot keeps the
+    // streams within the device's hardware work queues, so no two slots'
+    // kernels serialise behind each other.
     std::vector<cudaStream_t> streams;
+    int n_hi = 0;
     std::vector<cudaEvent_t> slot_done;    // completion of the slot's work
     std::vector<uint8_t *> slot_host;      // pinned staging (root, rows, nodes)
     std::vector<size_t> slot_host_bytes;
@@ -91,7 +114,20 @@ struct bz_server {
     bool notify = false;                   // completions are recorded once asked for
     std::mutex mu;
     std::condition_variable cv_work, cv_done;
-    std::deque<uint64_t> pending_commits, pending_opens;
+    // queued commits: by arrival (ids increase with arrival) and by size
+    std::set<uint64_t> pend_by_id;
+    std::set<std::pair<uint64_t, uint64_t>> pend_by_size;  // (bytes, id)
+    std::deque<uint64_t> pending_opens;
+    int admit_order = BZ_ADMIT_SMALLEST;
+    int64_t aging_ns = 500000000;      // 500 ms
+    int small_log = 20;                // requests of <= 2^small_log elements: high priority
+    std::atomic<uint64_t> wakes{0};    // bumped by the slots' host callbacks
+    // The server's own stream-ordered pool.  Its memory is reused across the
+    // slots' streams only once the freeing stream's work is known complete:
+    // with the default pool's internal dependencies, a small request's
+    // allocation could take memory a large request freed and be made to wait
+    // for that request's stream.
+    cudaMemPool_t pool = nullptr;
     std::map<uint64_t, std::unique_ptr<Request>> reqs;
     std::vector<uint64_t> running;  // commit or open in flight
     uint64_t next_id = 1;
@@ -163,60 +199,33 @@ int ensure_slot_host(bz_server *S, int slot, size_t bytes) {
     return BZ_OK;
 }
 
-// Start a commit on a free slot (caller holds the lock).
-int start_commit(bz_server *S, Request *r, int slot) {
-    bz_ctx *ctx = S->ctx;
-    cudaStream_t st = S->streams[slot];
-    const Shape &s = r->shape;
-    cudaError_t e = cudaMallocAsync((void **)&r->d_msg, s.msg_words() * 16, st);
-    if (e != cudaSuccess) return BZ_ERR_NOMEM;
-    bz_commitment *c = new bz_commitment();
-    c->ctx = ctx;
-    c->shape = s;
-    c->cw_bytes = s.cw_words() * 16;
-    c->tree_bytes = s.tree_nodes() * 32;
-    e = cudaMallocAsync((void **)&c->d_cw, c->cw_bytes, st);
-    if (e == cudaSuccess) e = cudaMallocAsync((void **)&c->d_tree, c->tree_bytes, st);
-    if (e != cudaSuccess) {
-        cudaGetLastError();
-        if (c->d_cw) cudaFreeAsync(c->d_cw, st);
-        cudaFreeAsync(r->d_msg, st);
-        r->d_msg = nullptr;
-        delete c;
-        return BZ_ERR_NOMEM;
-    }
-    r->commit = c;
-    cudaMemcpyAsync(r->d_msg, r->host_msg, s.msg_words() * 16, cudaMemcpyHostToDevice, st);
-    const uint4 *d_tw = nullptr;
-    int rc = get_twiddles(ctx, s.k_code(), &d_tw);
-    if (rc) return rc;
-    int n = launch_commit_kernels(ctx, s, schedule_for(ctx, s), r->d_msg, c->d_cw, c->d_tree,
-                                  d_tw, st, nullptr);
-    ctx->launches += (uint64_t)n;
-    cudaFreeAsync(r->d_msg, st);
-    r->d_msg = nullptr;
-    cudaMemcpyAsync(S->slot_host[slot], c->d_tree + (s.tree_nodes() - 1) * 32, 32,
-                    cudaMemcpyDeviceToHost, st);
-    cudaEventRecord(S->slot_done[slot], st);
-    e = cudaGetLastError();
-    if (e != cudaSuccess) return BZ_ERR_CUDA;
-    return BZ_OK;
+#ifndef BZ_SERVE_SHORT_CTAS
+#define BZ_SERVE_SHORT_CTAS 1
+#endif
+
+bool is_large(const bz_server *S, const Shape &s) { return s.log_msg_len > S->small_log; }
+
+// Wakes the scheduler once a slot's work is done (runs on a CUDA callback
+// thread: no CUDA call and no lock here; the scheduler's wait has a short
+// timeout as well, so a wakeup that races its check costs that timeout).
+void CUDART_CB slot_done_cb(void *p) {
+    bz_server *S = static_cast<bz_server *>(p);
+    S->wakes.fetch_add(1, std::memory_order_release);
+    S->cv_work.notify_one();
 }
 
-int start_open(bz_server *S, Request *r, int slot) {
+// Enqueue the gather of r's opened rows and multi-proof nodes and their copy
+// into the slot's pinned staging at byte offset h_off (rows, then nodes).
+int enqueue_open(bz_server *S, Request *r, cudaStream_t st, uint8_t *h) {
     bz_ctx *ctx = S->ctx;
-    cudaStream_t st = S->streams[slot];
     const Shape &s = r->shape;
     const size_t q = r->positions.size(), nn = r->node_idx.size();
     const size_t row_bytes = s.leaf_bytes();
-    // pinned staging: rows then nodes; device: positions, node indices,
-    // rows, nodes in one stream-ordered allocation
-    int rc = ensure_slot_host(S, slot, q * row_bytes + nn * 32 + 32);
-    if (rc) return rc;
+    // device: positions, node indices, rows, nodes in one stream-ordered allocation
     const size_t o_idx = q * 8, o_rows = (o_idx + nn * 8 + 15) & ~(size_t)15;
     const size_t o_nodes = o_rows + q * row_bytes, dev_bytes = o_nodes + nn * 32 + 16;
     uint8_t *d = nullptr;
-    if (cudaMallocAsync((void **)&d, dev_bytes, st) != cudaSuccess) {
+    if (cudaMallocFromPoolAsync((void **)&d, dev_bytes, S->pool, st) != cudaSuccess) {
         cudaGetLastError();
         return BZ_ERR_NOMEM;
     }
@@ -228,16 +237,132 @@ int start_open(bz_server *S, Request *r, int slot) {
     int n = launch_gather_rows(r->commit->d_cw, s.log_lanes, d_pos, q, d_rows, st);
     n += launch_gather_nodes(r->commit->d_tree, d_idx, nn, d_nodes, st);
     ctx->launches += (uint64_t)n;
-    uint8_t *h = S->slot_host[slot];
     if (q) cudaMemcpyAsync(h, d_rows, q * row_bytes, cudaMemcpyDeviceToHost, st);
     if (nn) cudaMemcpyAsync(h + q * row_bytes, d_nodes, nn * 32, cudaMemcpyDeviceToHost, st);
     cudaFreeAsync(d, st);
+    return BZ_OK;
+}
+
+// dst[i] = src[i], src in host memory the device can read (pinned, mapped).
+__global__ void __launch_bounds__(256) upload_kernel(const uint4 *__restrict__ src,
+                                                     uint4 *__restrict__ dst, uint64_t n) {
+    const uint64_t stride = (uint64_t)gridDim.x * blockDim.x;
+    uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    for (; i + 3 * stride < n; i += 4 * stride) {
+        const uint4 a = src[i], b = src[i + stride], c = src[i + 2 * stride],
+                    d = src[i + 3 * stride];
+        dst[i] = a;
+        dst[i + stride] = b;
+        dst[i + 2 * stride] = c;
+        dst[i + 3 * stride] = d;
+    }
+    for (; i < n; i += stride) dst[i] = src[i];
+}
+
+// The device's view of a host buffer, if it is pinned and mapped (null for
+// pageable memory or a failed query).
+const void *mapped_view(const void *host) {
+    cudaPointerAttributes a;
+    if (cudaPointerGetAttributes(&a, host) != cudaSuccess) {
+        cudaGetLastError();
+        return nullptr;
+    }
+    return a.type == cudaMemoryTypeHost ? a.devicePointer : nullptr;
+}
+
+size_t open_staging_bytes(const Request *r) {
+    return r->positions.size() * r->shape.leaf_bytes() + r->node_idx.size() * 32;
+}
+
+// Start a commit on a free slot (caller holds the lock).  A commit-then-open
+// request's opening follows on the same stream; the root lands in the first
+// 32 bytes of the slot's staging, the opening's rows and nodes after it.
+int start_commit(bz_server *S, Request *r, int slot) {
+    bz_ctx *ctx = S->ctx;
+    const Shape &s = r->shape;
+    const bool large = is_large(S, s);
+    cudaStream_t st = S->streams[slot];
+    if (r->auto_open) {
+        const int rc = ensure_slot_host(S, slot, 32 + open_staging_bytes(r));
+        if (rc) return rc;
+    }
+    cudaError_t e = cudaMallocFromPoolAsync((void **)&r->d_msg, s.msg_words() * 16, S->pool, st);
+    if (e != cudaSuccess) return BZ_ERR_NOMEM;
+    bz_commitment *c = new bz_commitment();
+    c->ctx = ctx;
+    c->shape = s;
+    c->cw_bytes = s.cw_words() * 16;
+    c->tree_bytes = s.tree_nodes() * 32;
+    e = cudaMallocFromPoolAsync((void **)&c->d_cw, c->cw_bytes, S->pool, st);
+    if (e == cudaSuccess)
+        e = cudaMallocFromPoolAsync((void **)&c->d_tree, c->tree_bytes, S->pool, st);
+    if (e != cudaSuccess) {
+        cudaGetLastError();
+        if (c->d_cw) cudaFreeAsync(c->d_cw, st);
+        cudaFreeAsync(r->d_msg, st);
+        r->d_msg = nullptr;
+        delete c;
+        return BZ_ERR_NOMEM;
+    }
+    r->commit = c;
+    // A small request's message is read from pinned host memory by a copy
+    // kernel on its high-priority stream (as fast as the copy engine, both
+    // being limited by the host link), so it never waits on the copy engine
+    // behind a large request's upload.  Large and pageable messages go
+    // through the copy engine.
+    const void *dev_view = large ? nullptr : mapped_view(r->host_msg);
+    if (dev_view) {
+        const uint64_t n = s.msg_words();
+        const unsigned grid = (unsigned)std::max<uint64_t>(
+            1, std::min<uint64_t>((uint64_t)ctx->num_sms, (n + 1023) / 1024));
+        upload_kernel<<<grid, 256, 0, st>>>(static_cast<const uint4 *>(dev_view), r->d_msg, n);
+        ctx->launches += 1;
+    } else {
+        cudaMemcpyAsync(r->d_msg, r->host_msg, s.msg_words() * 16, cudaMemcpyHostToDevice, st);
+    }
+    const uint4 *d_tw = nullptr;
+    int rc = get_twiddles(ctx, s.k_code(), &d_tw);
+    if (rc) return rc;
+    // a large request's table passes run as short CTAs when small requests
+    // have priority, so their kernels get SMs within a fraction of a pass
+    uint32_t schedule = schedule_for(ctx, s);
+#if BZ_SERVE_SHORT_CTAS
+    if (S->small_log >= 0 && large) schedule |= SCHED_SHORT_CTAS;
+#endif
+    int n = launch_commit_kernels(ctx, s, schedule, r->d_msg, c->d_cw, c->d_tree, d_tw, st,
+                                  nullptr);
+    ctx->launches += (uint64_t)n;
+    cudaFreeAsync(r->d_msg, st);
+    r->d_msg = nullptr;
+    cudaMemcpyAsync(S->slot_host[slot], c->d_tree + (s.tree_nodes() - 1) * 32, 32,
+                    cudaMemcpyDeviceToHost, st);
+    r->fused_open = false;
+    if (r->auto_open) {
+        rc = enqueue_open(S, r, st, S->slot_host[slot] + 32);
+        if (rc) return rc;
+        r->fused_open = true;
+    }
     cudaEventRecord(S->slot_done[slot], st);
+    cudaLaunchHostFunc(st, slot_done_cb, S);
+    e = cudaGetLastError();
+    if (e != cudaSuccess) return BZ_ERR_CUDA;
+    return BZ_OK;
+}
+
+int start_open(bz_server *S, Request *r, int slot) {
+    cudaStream_t st = S->streams[slot];
+    int rc = ensure_slot_host(S, slot, open_staging_bytes(r) + 32);
+    if (rc) return rc;
+    rc = enqueue_open(S, r, st, S->slot_host[slot]);
+    if (rc) return rc;
+    cudaEventRecord(S->slot_done[slot], st);
+    cudaLaunchHostFunc(st, slot_done_cb, S);
     return cudaGetLastError() == cudaSuccess ? BZ_OK : BZ_ERR_CUDA;
 }
 
 void free_commit_buffers(bz_server *S, Request *r, int slot) {
     if (r->commit) {
+        // the slot's work on these buffers is complete (its event was seen)
         cudaStream_t st = S->streams[slot >= 0 ? slot : 0];
         cudaFreeAsync(r->commit->d_cw, st);
         cudaFreeAsync(r->commit->d_tree, st);
@@ -246,17 +371,48 @@ void free_commit_buffers(bz_server *S, Request *r, int slot) {
     }
 }
 
-int free_slot(bz_server *S) {
-    for (int i = 0; i < S->n_slots; ++i)
+// High-priority slots while small requests have priority: half of them.
+int hi_slots(const bz_server *S) { return S->small_log >= 0 ? S->n_hi : 0; }
+
+// A free slot for a request (-1: none): large requests take the
+// normal-priority slots only, small ones (and openings) prefer the
+// high-priority ones.
+int free_slot(bz_server *S, bool large) {
+    const int h = hi_slots(S);
+    if (!large)
+        for (int i = 0; i < h; ++i)
+            if (!S->slot_busy[i]) return i;
+    for (int i = h; i < S->n_slots; ++i)
         if (!S->slot_busy[i]) return i;
     return -1;
+}
+
+// The next queued commit to admit and its slot ({0, -1}: none now): the
+// oldest when it has waited past the aging bound (or in arrival order), else
+// the smallest; a large request with no free normal-priority slot gives way
+// to the smallest small one.
+std::pair<uint64_t, int> next_commit(bz_server *S) {
+    const uint64_t oldest = *S->pend_by_id.begin();
+    uint64_t id = oldest;
+    if (S->admit_order == BZ_ADMIT_SMALLEST && S->ns() - S->reqs[oldest]->t_submit <= S->aging_ns)
+        id = S->pend_by_size.begin()->second;
+    bool large = is_large(S, S->reqs[id]->shape);
+    int slot = free_slot(S, large);
+    if (slot < 0 && large) {
+        id = S->pend_by_size.begin()->second;
+        large = is_large(S, S->reqs[id]->shape);
+        slot = large ? -1 : free_slot(S, false);
+    }
+    return slot < 0 ? std::make_pair((uint64_t)0, -1) : std::make_pair(id, slot);
 }
 
 void scheduler(bz_server *S) {
     cudaSetDevice(S->ctx->device);
     std::unique_lock<std::mutex> lk(S->mu);
+    uint64_t seen_wakes = 0;
     while (!S->stop) {
         bool progress = false;
+        seen_wakes = S->wakes.load(std::memory_order_acquire);
         // 1. completions
         for (size_t i = 0; i < S->running.size();) {
             Request *r = S->reqs[S->running[i]].get();
@@ -268,6 +424,18 @@ void scheduler(bz_server *S) {
             progress = true;
             S->slot_busy[r->slot] = false;
             const uint8_t *h = S->slot_host[r->slot];
+            auto take_opening = [&](const uint8_t *src) {
+                const size_t q_rows = r->positions.size(), nn = r->node_idx.size();
+                const size_t row_words = (size_t)2 << r->shape.log_lanes;
+                r->rows.assign((const uint64_t *)src, (const uint64_t *)src + q_rows * row_words);
+                r->nodes.assign(src + q_rows * row_words * 8,
+                                src + q_rows * row_words * 8 + nn * 32);
+                r->state = RS_OPENED;
+                r->t_opened = S->ns();
+                free_commit_buffers(S, r, r->slot);
+                S->in_use -= r->bytes - r->shape.msg_words() * 16;
+                ++S->n_opened;
+            };
             if (q != cudaSuccess) {
                 cudaGetLastError();
                 r->state = RS_FAILED;
@@ -281,31 +449,28 @@ void scheduler(bz_server *S) {
                 r->t_committed = S->ns();
                 S->in_use -= r->shape.msg_words() * 16;  // staging buffer released
                 ++S->n_committed;
-                if (r->auto_open) {
+                if (r->fused_open) {
+                    // the opening ran behind the commit on the same stream
+                    if (S->notify) S->completed.emplace_back(r->id, RS_COMMITTED);
+                    r->t_open_submit = r->t_committed;
+                    take_opening(h + 32);
+                } else if (r->auto_open) {
                     if (S->notify) S->completed.emplace_back(r->id, RS_COMMITTED);
                     r->state = RS_OPEN_QUEUED;
                     r->t_open_submit = r->t_committed;
                     S->pending_opens.push_back(r->id);
                 }
             } else if (r->state == RS_OPENING) {
-                const size_t q_rows = r->positions.size(), nn = r->node_idx.size();
-                const size_t row_words = (size_t)2 << r->shape.log_lanes;
-                r->rows.assign((const uint64_t *)h, (const uint64_t *)h + q_rows * row_words);
-                r->nodes.assign(h + q_rows * row_words * 8, h + q_rows * row_words * 8 + nn * 32);
-                r->state = RS_OPENED;
-                r->t_opened = S->ns();
-                free_commit_buffers(S, r, r->slot);
-                S->in_use -= r->bytes - r->shape.msg_words() * 16;
-                ++S->n_opened;
+                take_opening(h);
             }
-            if (S->notify && !(r->auto_open && r->state == RS_OPEN_QUEUED))
+            if (S->notify && r->state != RS_OPEN_QUEUED)
                 S->completed.emplace_back(r->id, r->state);
             S->running[i] = S->running.back();
             S->running.pop_back();
         }
         // 2. openings first (they free memory)
         while (!S->pending_opens.empty()) {
-            const int slot = free_slot(S);
+            const int slot = free_slot(S, false);
             if (slot < 0) break;
             Request *r = S->reqs[S->pending_opens.front()].get();
             S->pending_opens.pop_front();
@@ -324,13 +489,16 @@ void scheduler(bz_server *S) {
             S->running.push_back(r->id);
             progress = true;
         }
-        // 3. admit commits in arrival order while a slot and memory are free
-        while (!S->pending_commits.empty()) {
-            const int slot = free_slot(S);
-            if (slot < 0) break;
-            Request *r = S->reqs[S->pending_commits.front()].get();
+        // 3. admit commits while a slot and memory are free
+        while (!S->pend_by_id.empty()) {
+            const auto next = next_commit(S);
+            if (next.second < 0) break;  // no slot for any queued request now
+            const uint64_t id = next.first;
+            const int slot = next.second;
+            Request *r = S->reqs[id].get();
             if (S->in_use + r->bytes > S->budget) break;  // wait for openings to free HBM
-            S->pending_commits.pop_front();
+            S->pend_by_id.erase(id);
+            S->pend_by_size.erase({r->bytes, id});
             S->in_use += r->bytes;
             r->slot = slot;
             r->state = RS_RUNNING;
@@ -350,12 +518,14 @@ void scheduler(bz_server *S) {
             progress = true;
         }
         if (progress) S->cv_done.notify_all();
-        if (S->running.empty() && S->pending_commits.empty() && S->pending_opens.empty()) {
+        if (S->running.empty() && S->pend_by_id.empty() && S->pending_opens.empty()) {
             S->cv_work.wait_for(lk, std::chrono::milliseconds(50));
         } else if (!progress) {
-            lk.unlock();
-            std::this_thread::sleep_for(std::chrono::microseconds(20));
-            lk.lock();
+            // a slot's host callback or a submission wakes this; the timeout
+            // covers a callback that ran between the check and the wait
+            S->cv_work.wait_for(lk, std::chrono::microseconds(200), [&] {
+                return S->stop || S->wakes.load(std::memory_order_acquire) != seen_wakes;
+            });
         }
     }
 }
@@ -372,21 +542,41 @@ int bz_server_create(bz_ctx *ctx, int n_slots, uint64_t mem_budget_bytes, size_t
     S->n_slots = n_slots;
     S->budget = mem_budget_bytes ? mem_budget_bytes : ctx->budget;
     S->queue_cap = queue_cap ? queue_cap : 1 << 20;
-    S->streams.resize(n_slots);
-    S->slot_done.resize(n_slots);
+    S->streams.assign(n_slots, nullptr);
+    S->n_hi = n_slots / 2;
+    S->slot_done.assign(n_slots, nullptr);
     S->slot_host.assign(n_slots, nullptr);
     S->slot_host_bytes.assign(n_slots, 0);
     S->slot_busy.assign(n_slots, false);
+    int least = 0, greatest = 0;
+    cudaDeviceGetStreamPriorityRange(&least, &greatest);
+    cudaMemPoolProps props = {};
+    props.allocType = cudaMemAllocationTypePinned;
+    props.location.type = cudaMemLocationTypeDevice;
+    props.location.id = ctx->device;
+    uint64_t keep = UINT64_MAX;
+    int no = 0;
+    if (cudaMemPoolCreate(&S->pool, &props) != cudaSuccess ||
+        cudaMemPoolSetAttribute(S->pool, cudaMemPoolAttrReleaseThreshold, &keep) != cudaSuccess ||
+        cudaMemPoolSetAttribute(S->pool, cudaMemPoolReuseAllowInternalDependencies, &no) !=
+            cudaSuccess) {
+        cudaGetLastError();
+        if (S->pool) cudaMemPoolDestroy(S->pool);
+        delete S;
+        return BZ_ERR_CUDA;
+    }
     for (int i = 0; i < n_slots; ++i) {
-        if (cudaStreamCreateWithFlags(&S->streams[i], cudaStreamNonBlocking) != cudaSuccess ||
+        if (cudaStreamCreateWithPriority(&S->streams[i], cudaStreamNonBlocking,
+                                         i < S->n_hi ? greatest : least) != cudaSuccess ||
             cudaEventCreateWithFlags(&S->slot_done[i], cudaEventDisableTiming) != cudaSuccess ||
-            ensure_slot_host(S, i, 64 << 10) != BZ_OK) {
+            ensure_slot_host(S, i, 1 << 20) != BZ_OK) {
             cudaGetLastError();
             for (int j = 0; j <= i; ++j) {
                 if (S->streams[j]) cudaStreamDestroy(S->streams[j]);
                 if (S->slot_done[j]) cudaEventDestroy(S->slot_done[j]);
                 if (S->slot_host[j]) cudaFreeHost(S->slot_host[j]);
             }
+            cudaMemPoolDestroy(S->pool);
             delete S;
             return BZ_ERR_CUDA;
         }
@@ -394,6 +584,18 @@ int bz_server_create(bz_ctx *ctx, int n_slots, uint64_t mem_budget_bytes, size_t
     S->t0 = Clock::now();
     S->thr = std::thread(scheduler, S);
     *out = S;
+    return BZ_OK;
+}
+
+int bz_server_set_policy(bz_server *S, int admit_order, uint32_t aging_ms,
+                         int high_priority_log_size) {
+    if (!S || (admit_order != BZ_ADMIT_FIFO && admit_order != BZ_ADMIT_SMALLEST) ||
+        high_priority_log_size < -1 || high_priority_log_size > 62)
+        return BZ_ERR_ARG;
+    std::lock_guard<std::mutex> g(S->mu);
+    S->admit_order = admit_order;
+    S->aging_ns = (int64_t)aging_ms * 1000000;
+    S->small_log = high_priority_log_size;
     return BZ_OK;
 }
 
@@ -419,11 +621,12 @@ int submit(bz_server *S, const uint64_t *host_msg, size_t n_words, const bz_para
         r->auto_open = true;
     }
     std::lock_guard<std::mutex> g(S->mu);
-    if (S->pending_commits.size() >= S->queue_cap) return BZ_ERR_BUSY;
+    if (S->pend_by_id.size() >= S->queue_cap) return BZ_ERR_BUSY;
     r->id = S->next_id++;
     r->t_submit = S->ns();
     *request_id = r->id;
-    S->pending_commits.push_back(r->id);
+    S->pend_by_id.insert(r->id);
+    S->pend_by_size.insert({r->bytes, r->id});
     S->reqs[r->id] = std::move(r);
     S->cv_work.notify_one();
     return BZ_OK;
@@ -571,7 +774,7 @@ int bz_server_stats(bz_server *S, uint64_t *committed, uint64_t *opened, uint64_
     if (opened) *opened = S->n_opened;
     if (failed) *failed = S->n_failed;
     if (in_use) *in_use = S->in_use;
-    if (queued) *queued = S->pending_commits.size() + S->pending_opens.size();
+    if (queued) *queued = S->pend_by_id.size() + S->pending_opens.size();
     return BZ_OK;
 }
 
@@ -592,6 +795,7 @@ int bz_server_destroy(bz_server *S) {
         cudaStreamSynchronize(s);
         cudaStreamDestroy(s);
     }
+    cudaMemPoolDestroy(S->pool);
     for (int i = 0; i < S->n_slots; ++i) {
         cudaEventDestroy(S->slot_done[i]);
         cudaFreeHost(S->slot_host[i]);

@@ -233,14 +233,28 @@ enum {
 };
 int bz_server_create(bz_ctx *ctx, int n_slots, uint64_t mem_budget_bytes, size_t queue_cap,
                      bz_server **out);
+/* Scheduling policy (no counterpart in the reference, which has no server).
+ * admit_order: BZ_ADMIT_SMALLEST (the default) admits the smallest queued
+ * commit first, unless the oldest has waited more than aging_ms (default 500),
+ * which then goes first; BZ_ADMIT_FIFO admits in arrival order.  Requests of
+ * at most 2^high_priority_log_size elements (default 20; -1: no priorities)
+ * run on the high-priority half of the slots (and on the other half when
+ * those are busy); larger requests run on the other half only, their table
+ * passes cut into short CTAs, so a small request's kernels take SMs within a
+ * fraction of a large commit's pass.  A commit-then-open request's opening
+ * always runs right behind its commit on the same stream. */
+enum { BZ_ADMIT_FIFO = 0, BZ_ADMIT_SMALLEST = 1 };
+int bz_server_set_policy(bz_server *s, int admit_order, uint32_t aging_ms,
+                         int high_priority_log_size);
 /* host_msg must stay valid until the request reaches BZ_REQ_COMMITTED
  * (pinned host memory gives overlapped copies).  BZ_ERR_BUSY when the queue
  * holds queue_cap commits. */
 int bz_server_submit_commit(bz_server *s, const uint64_t *host_msg, size_t n_words,
                             const bz_params *params, uint64_t *request_id);
-/* Commit-then-open as one request: the opening at the q positions is queued
- * as soon as the commit completes (same results as submit_commit followed by
- * submit_open).  BZ_ERR_ARG for a position outside the codeword. */
+/* Commit-then-open as one request: the opening at the q positions runs right
+ * behind the commit (same results as submit_commit followed by submit_open);
+ * the completion queue reports COMMITTED and OPENED together.  BZ_ERR_ARG for
+ * a position outside the codeword. */
 int bz_server_submit_commit_open(bz_server *s, const uint64_t *host_msg, size_t n_words,
                                  const bz_params *params, const uint64_t *positions, size_t q,
                                  uint64_t *request_id);

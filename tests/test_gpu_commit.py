@@ -68,7 +68,7 @@ SCHEDULES = [0, 1, 2, 3, 4, 0x10, 0x13, 0x20,
              0x1000 | 2, 0x1200 | 2, 0x1000 | (1 << 10) | 2, 0x1000 | 0, 0x3602, 0x3a03,
              (1 << 10), (2 << 10) | 0x200, (3 << 10) | 0x3200, 0x1200 | (1 << 10), 0x3200,
              0x4000, 0x5000, 0x5400, 0x5C00, 0x5001, 0x5002, 0x4010,
-             0x8000, 0x18000]
+             0x8000, 0x18000, 0x208000, 0x205000]
 
 
 @pytest.mark.parametrize("schedule", SCHEDULES)
@@ -104,7 +104,7 @@ def test_roots_fixture(ctx):
         assert c.root.hex() == e["root"], e
 
 
-@pytest.mark.parametrize("schedule", [0x5000, 0x5400, 0x5001, 0x8000, 0x18000])
+@pytest.mark.parametrize("schedule", [0x5000, 0x5400, 0x5001, 0x8000, 0x18000, 0x208000])
 def test_compact_twiddle_tables_at_benchmark_shapes(ctx, schedule):
     """Compact tables for the narrow twiddles of the deepest radix-4 pass
     (all three twiddles at 2^20 and 2^24, the second layer's only at 2^28

@@ -112,6 +112,39 @@ def test_server_admission_by_memory(oracle, ctx):
         srv.wait(b, OPENED, 60000)
 
 
+@pytest.mark.parametrize("order", ["smallest", "fifo"])
+def test_server_admission_order(oracle, ctx, order):
+    """One slot: while a large commit runs, a large and then a small request
+    queue up.  Smallest-first admits the small one first; arrival order (or
+    an aging bound already passed) the large one.  Results are unchanged."""
+    from bitz_gb300 import PcsParams
+    from bitz_gb300.serve import ADMIT_FIFO, ADMIT_SMALLEST, OPENED, Server
+
+    big, small = PcsParams(22 + 7, 2, 11, 1), PcsParams(12 + 7, 2, 6, 1)
+    m_big = [oracle.chacha_words(40 + i, 1 << 22) for i in range(2)]
+    m_small = oracle.chacha_words(42, 1 << 12)
+    with Server(ctx, n_slots=1) as srv:
+        srv.set_policy(ADMIT_SMALLEST if order == "smallest" else ADMIT_FIFO, 10000, 20)
+        a = srv.submit_commit_open(m_big[0], big, [0, 3])
+        b = srv.submit_commit_open(m_big[1], big, [1])
+        c = srv.submit_commit_open(m_small, small, [2, 5])
+        for rid in (a, b, c):
+            srv.wait(rid, OPENED, 120000)
+        tb, tc = srv.times(b)[1], srv.times(c)[1]
+        assert (tc < tb) == (order == "smallest")
+        for rid, m, p, q in ((b, m_big[1], big, [1]), (c, m_small, small, [2, 5])):
+            cw, tree, root = oracle.commit(m, 2, p.log_batch_size, 1, n_threads=8)
+            assert srv.root(rid) == root
+            rows, proof = srv.open_result(rid, p.num_ntts())
+            want = cw.reshape(-1, p.num_ntts(), 2)[q]
+            assert (rows == want).all()
+    with Server(ctx, n_slots=1) as srv:
+        with pytest.raises(Exception):
+            srv.set_policy(7, 10, 20)
+        with pytest.raises(Exception):
+            srv.set_policy(ADMIT_FIFO, 10, 63)
+
+
 def test_server_bounded_wait_times_out(ctx):
     from bitz_gb300 import BzError, PcsParams
     from bitz_gb300.serve import OPENED, Server
