@@ -323,9 +323,12 @@ int start_commit(bz_server *S, Request *r, int slot) {
     const uint4 *d_tw = nullptr;
     int rc = get_twiddles(ctx, s.k_code(), &d_tw);
     if (rc) return rc;
-    // a large request's table passes run as short CTAs when small requests
-    // have priority, so their kernels get SMs within a fraction of a pass
-    uint32_t schedule = schedule_for(ctx, s);
+    // The shape's default schedule, not one the context's autotuner picked:
+    // those are timed alone and may run two streams of their own (pipelined
+    // schedules), which would bypass the slot's priority.  A large request's
+    // table passes run as short CTAs when small requests have priority, so
+    // their kernels get SMs within a fraction of a pass.
+    uint32_t schedule = default_schedule(s);
 #if BZ_SERVE_SHORT_CTAS
     if (S->small_log >= 0 && large) schedule |= SCHED_SHORT_CTAS;
 #endif
