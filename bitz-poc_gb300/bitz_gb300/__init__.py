@@ -27,3 +27,4 @@ from . import codec  # noqa: F401,E402
 from .binary_pcs import BinaryPcs, BitMleOpening, Round0Prover  # noqa: F401,E402
 from . import ingest  # noqa: F401,E402
 from . import shard  # noqa: F401,E402
+from . import gkr  # noqa: F401,E402

@@ -137,6 +137,9 @@ _SIGS = {
     "bz_rows_from_packed_cols": (_I, [_P, _P, _U32, _U32, _P]),
     "bz_commit_rows": (_I, [_P, _P, _U32, _U32, _U32, _U32, _U32, _PP, _P]),
     "bz_commit_shard": (_I, [_P, _P, _S, ctypes.POINTER(Params), _U32, _U32, _PP]),
+    "bz_gkr_prove": (_I, [_P, _P, _S, _S, _P, _P, _P, _P, _P, _P]),
+    "bz_gkr_prove_device": (_I, [_P, _P, _S, _S, _P, _P, _P, _P, _P, _P]),
+    "bz_gkr_forest_prove": (_I, [_P, _P, _P, _I, _I, _P, _P, _P, _P, _P, _P]),
     "bz_commit_shard_device": (_I, [_P, _P, _S, ctypes.POINTER(Params), _U32, _U32, _PP]),
     "bz_commitment_leaf_cvs": (_I, [_P, _P, _S]),
     "bz_merkle_from_shards": (_I, [_P, _P, _U32, ctypes.POINTER(Params), _PP, _P]),

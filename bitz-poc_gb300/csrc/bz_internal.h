@@ -169,6 +169,20 @@ int launch_phi(const uint4 *d_eq_hi, size_t n, const uint4 *d_eq_r2, uint4 *d_ou
 int launch_chacha(uint64_t seed, uint64_t first_word, uint4 *d_out, size_t n_words,
                   cudaStream_t st);
 
+// Batched grand-product GKR (BitZ src/bitz/gkr.rs; fold.cu): one product
+// layer (out[i] = in[i] * in[half + i]), one dense round over h slots of the
+// two half tables (with the previous round's fold by rho first when `fold`;
+// the reduced (sum_end, sum_inf) land in d_out[0..3]; d_w_next, when not
+// null, gets the next round's weights), and the forest's leaf grid.
+// d_partials holds fold_partials_bytes(0) bytes.
+int launch_gkr_product(const uint4 *d_in, size_t half, uint4 *d_out, cudaStream_t st,
+                       int num_sms);
+int launch_gkr_round(uint4 *d_l, uint4 *d_r, const uint4 *d_w, size_t h, bool fold, uint4 rho,
+                     bool send_one, uint4 *d_w_next, uint64_t *d_partials, uint64_t *d_out,
+                     cudaStream_t st, int num_sms);
+int launch_gkr_forest_leaves(const uint64_t *d_packed, const uint4 *d_images, int t, int s,
+                             uint4 *d_out, cudaStream_t st, int num_sms);
+
 // Recursive Ligerito prover (ligerito.cu).  Induce: zero the 2^log_d domain,
 // scatter the nq query weights d_w at d_pos, apply the transposed forward NTT
 // with the twiddle heap of log_d; the low 2^log_msg_cols outputs are the

@@ -545,7 +545,10 @@ __global__ void __launch_bounds__(256) phi_kernel(const uint4 *eq_hi, uint64_t n
         out[y] = lc.mul(T, eq_hi[y]);
 }
 
+void init_gkr_kernels();
+
 void init_fold_kernels() {
+    init_gkr_kernels();
     cudaFuncSetAttribute(phi_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
                          (int)kRTableSmem);
     cudaFuncSetAttribute(eq_split_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
@@ -614,6 +617,123 @@ int launch_chacha(uint64_t seed, uint64_t first_word, uint4 *d_out, size_t n_wor
     const unsigned grid = (unsigned)std::min<uint64_t>((blocks + 255) / 256, 8192);
     chacha_kernel<<<grid, 256, 0, st>>>((uint32_t)seed, (uint32_t)(seed >> 32), first_word, d_out,
                                         n_words);
+    return 1;
+}
+
+// ---------------------------------------------------------------------------
+// Batched grand-product GKR (BitZ src/bitz/gkr.rs), the dense rounds.
+// ---------------------------------------------------------------------------
+// One product layer: out[i] = in[i] * in[half + i] (GrandProductCircuit::
+// batched_eval, gkr.rs:93-108: the top index bit pairs the factors).
+__global__ void __launch_bounds__(256) gkr_product_kernel(const uint4 *in, uint64_t half,
+                                                          uint4 *out) {
+    for (uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; i < half;
+         i += (uint64_t)gridDim.x * blockDim.x)
+        out[i] = gf_mul(in[i], in[half + i]);
+}
+
+// One dense round over h slots (prove_dense_rounds, gkr.rs:188-282, with the
+// column-free weights): the tables l and r (the layer's two halves) hold the
+// round's lo entries at [0, h) and hi entries at [h, 2h).  With FOLD the
+// previous round's challenge rho is applied first, in place: entries q0..q3
+// at c, h + c, 2h + c, 3h + c become q0 + rho (q2 - q0) at c and
+// q1 + rho (q3 - q1) at h + c (kernels.rs:146-186, 312-348).  Each CTA
+// stores its partial sums of w_c l_end r_end and w_c (l_hi - l_lo)(r_hi -
+// r_lo) (kernels.rs:248-262; l_end = l_hi when send_one), unreduced; the
+// finish kernel reduces them.  With w_next, the next round's weights
+// w_next[c] = w[c] + w[c + h/2] (eq over one coordinate fewer: the two
+// values of the dropped coordinate's factor sum to 1) are written too.
+template <bool FOLD>
+__global__ void __launch_bounds__(256, 2) gkr_round_kernel(uint4 *l, uint4 *r, const uint4 *w,
+                                                           uint64_t h, uint4 rho, int send_one,
+                                                           uint64_t *partials, uint4 *w_next) {
+    extern __shared__ uint4 smem[];
+    const char *T = nullptr;
+    T16Lane8 lc;
+    if constexpr (FOLD) {
+        T = build_r_table(smem, rho);
+        lc.init();
+    }
+    gf_wide e = gf_wide_zero(), f = gf_wide_zero();
+    const uint64_t stride = (uint64_t)gridDim.x * blockDim.x;
+    for (uint64_t c = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; c < h; c += stride) {
+        uint4 l0, l1, r0, r1;
+        if constexpr (FOLD) {
+            const uint4 a0 = l[c], a1 = l[h + c], a2 = l[2 * h + c], a3 = l[3 * h + c];
+            const uint4 b0 = r[c], b1 = r[h + c], b2 = r[2 * h + c], b3 = r[3 * h + c];
+            l0 = gf_add(a0, lc.mul(T, gf_add(a2, a0)));
+            l1 = gf_add(a1, lc.mul(T, gf_add(a3, a1)));
+            r0 = gf_add(b0, lc.mul(T, gf_add(b2, b0)));
+            r1 = gf_add(b1, lc.mul(T, gf_add(b3, b1)));
+            l[c] = l0;
+            l[h + c] = l1;
+            r[c] = r0;
+            r[h + c] = r1;
+        } else {
+            l0 = l[c];
+            l1 = l[h + c];
+            r0 = r[c];
+            r1 = r[h + c];
+        }
+        const uint4 wc = w[c];
+        if (w_next && c < h / 2) w_next[c] = gf_add(wc, w[c + h / 2]);
+        const uint4 le = send_one ? l1 : l0, re = send_one ? r1 : r0;
+        gf_wide_xor(e, gf_mul_wide(gf_mul(wc, le), re));
+        gf_wide_xor(f, gf_mul_wide(gf_mul(wc, gf_add(l1, l0)), gf_add(r1, r0)));
+    }
+    cta_store_pair(e, f, partials + (uint64_t)blockIdx.x * 8);
+}
+
+// The leaf grid of the BitZ forest (src/bitz/forest_tests.rs:42-68): leaf
+// row * 2^s + column is images[row] when bit (column mod 64) of
+// packed[(column / 64) * 2^t + row] is set, else 1.
+__global__ void __launch_bounds__(256) gkr_forest_leaves_kernel(const uint64_t *packed,
+                                                                const uint4 *images, int t,
+                                                                int s, uint4 *out) {
+    const uint64_t n = (uint64_t)1 << (t + s), rows = (uint64_t)1 << t;
+    for (uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n;
+         i += (uint64_t)gridDim.x * blockDim.x) {
+        const uint64_t row = i >> s, col = i & (((uint64_t)1 << s) - 1);
+        const uint64_t bit = (packed[(col >> 6) * rows + row] >> (col & 63)) & 1;
+        out[i] = bit ? images[row] : make_uint4(1, 0, 0, 0);
+    }
+}
+
+int launch_gkr_product(const uint4 *d_in, size_t half, uint4 *d_out, cudaStream_t st,
+                       int num_sms) {
+    const unsigned grid = (unsigned)std::max<uint64_t>(
+        1, std::min<uint64_t>((half + 255) / 256, (uint64_t)num_sms * 8));
+    gkr_product_kernel<<<grid, 256, 0, st>>>(d_in, half, d_out);
+    return 1;
+}
+
+int gkr_round_grid(size_t h, int num_sms) { return std::min(msg_grid(h, num_sms), 1024); }
+
+int launch_gkr_round(uint4 *d_l, uint4 *d_r, const uint4 *d_w, size_t h, bool fold, uint4 rho,
+                     bool send_one, uint4 *d_w_next, uint64_t *d_partials, uint64_t *d_out,
+                     cudaStream_t st, int num_sms) {
+    const int grid = gkr_round_grid(h, num_sms);
+    if (fold)
+        gkr_round_kernel<true><<<grid, 256, kRTableSmem, st>>>(d_l, d_r, d_w, h, rho, send_one,
+                                                               d_partials, d_w_next);
+    else
+        gkr_round_kernel<false><<<grid, 256, 0, st>>>(d_l, d_r, d_w, h, rho, send_one,
+                                                      d_partials, d_w_next);
+    finish_msg_kernel<<<1, kFinishThreads, 0, st>>>(d_partials, grid, d_out);
+    return 2;
+}
+
+void init_gkr_kernels() {
+    cudaFuncSetAttribute(gkr_round_kernel<true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                         (int)kRTableSmem);
+}
+
+int launch_gkr_forest_leaves(const uint64_t *d_packed, const uint4 *d_images, int t, int s,
+                             uint4 *d_out, cudaStream_t st, int num_sms) {
+    const uint64_t n = (uint64_t)1 << (t + s);
+    const unsigned grid = (unsigned)std::max<uint64_t>(
+        1, std::min<uint64_t>((n + 255) / 256, (uint64_t)num_sms * 8));
+    gkr_forest_leaves_kernel<<<grid, 256, 0, st>>>(d_packed, d_images, t, s, d_out);
     return 1;
 }
 

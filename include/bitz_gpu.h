@@ -286,6 +286,44 @@ int bz_server_stats(bz_server *s, uint64_t *committed, uint64_t *opened, uint64_
                     uint64_t *in_use, uint64_t *queued);
 int bz_server_destroy(bz_server *s);
 
+/* ---- batched grand-product GKR (BitZ src/bitz/gkr.rs) -------------------- */
+/* The caller's transcript (the reference's spongefish ProverState stays on
+ * the caller's side): absorb the prover message msg[0..3] (two field
+ * elements, lo and hi words each) and write the next challenge; stage
+ * BZ_GKR_ROUND is the reference's Stage::GkrRound, BZ_GKR_CLOSE
+ * Stage::GkrClose (prover_message then native_scalar, gkr.rs:264-271).  A
+ * nonzero return aborts the proof with BZ_ERR_STATE. */
+enum { BZ_GKR_ROUND = 0, BZ_GKR_CLOSE = 1 };
+typedef int (*bz_gkr_transcript_fn)(void *user, int stage, const uint64_t msg[4],
+                                    uint64_t challenge[2]);
+/* gpgkr_prove (src/bitz/gkr.rs:113-125) of
+ * GrandProductCircuit::new(leaves).batched_eval(groups) (gkr.rs:80-108):
+ * n_leaves a power of two (the reference pads with ones; so must the
+ * caller), groups a power of two below it, point: log2(groups) field
+ * elements (little-endian), the claim point on the roots.  Writes the groups
+ * roots (NULL: skipped), the little-endian leaf point (log2(n_leaves)
+ * elements) and the claimed leaf value.  Messages, challenges, point and
+ * claim are the reference's for the same transcript.  Device memory: about
+ * 1.5 x the leaves besides them.  Synchronous. */
+int bz_gkr_prove(bz_ctx *ctx, const uint64_t *leaves, size_t n_leaves, size_t groups,
+                 const uint64_t *point, bz_gkr_transcript_fn fn, void *user,
+                 uint64_t *roots, uint64_t *out_point, uint64_t out_claim[2]);
+/* Same with the leaves in device memory; they are overwritten (the rounds
+ * fold the leaf layer in place, as the reference's batched_eval consumes
+ * its leaves). */
+int bz_gkr_prove_device(bz_ctx *ctx, uint64_t *d_leaves, size_t n_leaves, size_t groups,
+                        const uint64_t *point, bz_gkr_transcript_fn fn, void *user,
+                        uint64_t *roots, uint64_t *out_point, uint64_t out_claim[2]);
+/* Forest::prove (src/bitz/forest.rs:246-300) from its inputs: 2^t rows of
+ * 2^s columns, leaf (row, column) = images[row] where bit (column mod 64) of
+ * packed[(column / 64) * 2^t + row] is set, else 1 (the leaf grid of
+ * src/bitz/forest_tests.rs:42-68); zeta: s elements.  The same transcript
+ * as bz_gkr_prove over those leaves with 2^s groups, which is what the
+ * reference's forest matches byte for byte. */
+int bz_gkr_forest_prove(bz_ctx *ctx, const uint64_t *packed, const uint64_t *images, int t,
+                        int s, const uint64_t *zeta, bz_gkr_transcript_fn fn, void *user,
+                        uint64_t *roots, uint64_t *out_point, uint64_t out_claim[2]);
+
 /* ---- sumcheck folds (device buffers) ------------------------------------ */
 /* fold_and_msg_lsb (flock-core/src/pcs/ligerito.rs:2634-2735), used by
  * SumcheckProver::fold (:3046-3057): nf[j] = f[2j] + (f[2j]+f[2j+1])*r (same
