@@ -245,6 +245,25 @@ def cpu_baseline(n_threads: int, log_n: int = LOG_N):
     return (1 << log_n) / dt, dt, root, open_ms, bit_mle_ms
 
 
+def cpu_gkr_ms(t: int = 12, s: int = 10) -> float:
+    """The oracle's dense GKR prover (a CPU restatement of BitZ's gpgkr_prove,
+    its field arithmetic in C, its loops in numpy) on the same 2^(t+s)-leaf
+    forest as the GPU leg's first size, in ms."""
+    from oracle import gkr as G
+
+    rng = np.random.default_rng(77 + t)
+    rows, cols = 1 << t, 1 << s
+    packed = rng.integers(0, 2**64, ((cols + 63) // 64, rows), dtype=np.uint64)
+    images = rng.integers(0, 2**64, (rows, 2), dtype=np.uint64)
+    zeta = [rng.integers(0, 2**64, 2, dtype=np.uint64) for _ in range(s)]
+    t0 = time.perf_counter()
+    leaves = G.forest_leaves(packed, images, t, s)
+    _, wit = G.batched_eval(leaves, cols)
+    tr = G.HashChallenges(b"gkr-bench")
+    G.prove(tr.send, tr.challenge, zeta, wit)
+    return (time.perf_counter() - t0) * 1e3
+
+
 def run_reference(args, ws, rank):
     if rank != 0:
         return 0
@@ -488,6 +507,9 @@ def run_gpu(args, ws, rank, local):
         opening = None
         if not args.skip_open:
             opening = _bench_open(ctx, bz, msg, params)
+        gkr = None
+        if not args.skip_gkr:
+            gkr = _bench_gkr(ctx, bz)
 
         # ---- CPU baseline (oracle, all host threads, one full commit) -----
         cpu = None
@@ -499,6 +521,8 @@ def run_gpu(args, ws, rank, local):
                    "sample": CPU_PORT_SAMPLE.format(
                        what=f"one full 2^24-element commit ({dt:.2f} s)"),
                    "prove_ms": cpu_open_ms, "bit_mle_2^20_round0_and_open_ms": cpu_bit_mle_ms}
+            if not args.skip_gkr:
+                cpu["gkr_forest_2^22_ms"] = cpu_gkr_ms()
         sorted_ms = sorted(step_ms)
         p99 = sorted_ms[min(len(sorted_ms) - 1, int(round(0.99 * (len(sorted_ms) - 1))))]
         out = {
@@ -535,7 +559,7 @@ def run_gpu(args, ws, rank, local):
             "phase_share": {k: round(v[1] / total_phase, 4) for k, v in agg.items()},
             "clocks": clk, "gpu_launches": launches, "wall_s": wall,
             "schedule": schedule, "batched": batch, "serving": serve, "shapes": shapes,
-            "opening": opening, "cpu_baseline": cpu,
+            "opening": opening, "gkr_forest": gkr, "cpu_baseline": cpu,
         }
         print(json.dumps(out), flush=True)
     msg.free()
@@ -749,6 +773,54 @@ def _bench_bit_mle(ctx, bz):
     return out
 
 
+class _GkrTranscript:
+    """The library's host BLAKE3 transcript as the GKR prover's transcript:
+    each message is absorbed, each challenge is a field challenge."""
+
+    def __init__(self, bz):
+        self.t = bz.Blake3Transcript()
+        self.t.absorb(b"gkr-bench")
+
+    def send(self, stage, msg):
+        self.t.absorb(bytes([stage]) + b"".join(np.asarray(m, np.uint64).tobytes() for m in msg))
+
+    def challenge(self, stage):
+        return self.t.get_field_challenge()
+
+
+def _bench_gkr(ctx, bz):
+    """Forest::prove (the dense grand-product GKR over the forest's leaf grid)
+    at 2^27 leaves, the reference's own 2^27-bit forest (2^17 rows x 2^10
+    columns, src/bitz/forest.rs), and at 2^22: the leaf grid is built on the
+    device from the packed bits and the row images, then every layer's
+    rounds run on the GPU with the transcript on the host (BLAKE3, one
+    absorb and one challenge per round)."""
+    from bitz_gb300 import gkr as K
+
+    out = {}
+    for t, s, reps in ((12, 10, 5), (17, 10, 3)):
+        rng = np.random.default_rng(77 + t)
+        rows, cols = 1 << t, 1 << s
+        packed = rng.integers(0, 2**64, ((cols + 63) // 64, rows), dtype=np.uint64)
+        images = rng.integers(0, 2**64, (rows, 2), dtype=np.uint64)
+        zeta = [rng.integers(0, 2**64, 2, dtype=np.uint64) for _ in range(s)]
+        K.forest_prove(packed, images, t, s, zeta, _GkrTranscript(bz), ctx)   # warm
+        ms = []
+        for _ in range(reps):
+            tr = _GkrTranscript(bz)
+            t0 = time.perf_counter()
+            K.forest_prove(packed, images, t, s, zeta, tr, ctx)
+            ms.append((time.perf_counter() - t0) * 1e3)
+        rounds = sum(k + 1 for k in range(s, s + t))
+        out[f"2^{t + s}"] = {"ms": statistics.median(ms), "rows": rows, "cols": cols,
+                             "leaves": rows * cols, "transcript_rounds": rounds,
+                             "reps": reps}
+    out["note"] = ("wall time of bz_gkr_forest_prove through the Python API: leaf grid upload "
+                   "and build, product layers, every round's kernels and the mailbox post of "
+                   "its two sums, the host transcript called back into Python once per round")
+    return out
+
+
 def _geometric_sizes(rng, n, lo=14, hi=26, q=0.97):
     ks = np.arange(lo, hi + 1)
     w = q ** (ks - lo)
@@ -913,6 +985,7 @@ def main():
     ap.add_argument("--skip-serve", action="store_true")
     ap.add_argument("--skip-shapes", action="store_true")
     ap.add_argument("--skip-open", action="store_true")
+    ap.add_argument("--skip-gkr", action="store_true")
     ap.add_argument("--no-autotune", action="store_true")
     ap.add_argument("--schedule", default=None,
                     help="fixed NTT schedule for the headline shape (e.g. 0x1002) instead of "

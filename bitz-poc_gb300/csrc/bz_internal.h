@@ -174,12 +174,14 @@ int launch_chacha(uint64_t seed, uint64_t first_word, uint4 *d_out, size_t n_wor
 // two half tables (with the previous round's fold by rho first when `fold`;
 // the reduced (sum_end, sum_inf) land in d_out[0..3]; d_w_next, when not
 // null, gets the next round's weights), and the forest's leaf grid.
-// d_partials holds fold_partials_bytes(0) bytes.
+// d_partials holds fold_partials_bytes(0) bytes.  With `post` the round's
+// last CTA posts the sums to the mapped mailbox (as the sumcheck rounds do)
+// and d_out is unused.
 int launch_gkr_product(const uint4 *d_in, size_t half, uint4 *d_out, cudaStream_t st,
                        int num_sms);
 int launch_gkr_round(uint4 *d_l, uint4 *d_r, const uint4 *d_w, size_t h, bool fold, uint4 rho,
                      bool send_one, uint4 *d_w_next, uint64_t *d_partials, uint64_t *d_out,
-                     cudaStream_t st, int num_sms);
+                     cudaStream_t st, int num_sms, const MsgPost *post = nullptr);
 int launch_gkr_forest_leaves(const uint64_t *d_packed, const uint4 *d_images, int t, int s,
                              uint4 *d_out, cudaStream_t st, int num_sms);
 

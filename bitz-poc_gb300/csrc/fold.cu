@@ -646,7 +646,8 @@ __global__ void __launch_bounds__(256) gkr_product_kernel(const uint4 *in, uint6
 template <bool FOLD>
 __global__ void __launch_bounds__(256, 2) gkr_round_kernel(uint4 *l, uint4 *r, const uint4 *w,
                                                            uint64_t h, uint4 rho, int send_one,
-                                                           uint64_t *partials, uint4 *w_next) {
+                                                           uint64_t *partials, MsgMailbox mb,
+                                                           uint4 *w_next) {
     extern __shared__ uint4 smem[];
     const char *T = nullptr;
     T16Lane8 lc;
@@ -681,7 +682,7 @@ __global__ void __launch_bounds__(256, 2) gkr_round_kernel(uint4 *l, uint4 *r, c
         gf_wide_xor(e, gf_mul_wide(gf_mul(wc, le), re));
         gf_wide_xor(f, gf_mul_wide(gf_mul(wc, gf_add(l1, l0)), gf_add(r1, r0)));
     }
-    cta_store_pair(e, f, partials + (uint64_t)blockIdx.x * 8);
+    msg_finish_call(e, f, partials, mb);
 }
 
 // The leaf grid of the BitZ forest (src/bitz/forest_tests.rs:42-68): leaf
@@ -711,14 +712,17 @@ int gkr_round_grid(size_t h, int num_sms) { return std::min(msg_grid(h, num_sms)
 
 int launch_gkr_round(uint4 *d_l, uint4 *d_r, const uint4 *d_w, size_t h, bool fold, uint4 rho,
                      bool send_one, uint4 *d_w_next, uint64_t *d_partials, uint64_t *d_out,
-                     cudaStream_t st, int num_sms) {
+                     cudaStream_t st, int num_sms, const MsgPost *post) {
     const int grid = gkr_round_grid(h, num_sms);
+    MsgMailbox mb;
+    if (post) mb = {post->ticket, post->words, post->seq, post->seq_val};
     if (fold)
         gkr_round_kernel<true><<<grid, 256, kRTableSmem, st>>>(d_l, d_r, d_w, h, rho, send_one,
-                                                               d_partials, d_w_next);
+                                                               d_partials, mb, d_w_next);
     else
         gkr_round_kernel<false><<<grid, 256, 0, st>>>(d_l, d_r, d_w, h, rho, send_one,
-                                                      d_partials, d_w_next);
+                                                      d_partials, mb, d_w_next);
+    if (post) return 1;
     finish_msg_kernel<<<1, kFinishThreads, 0, st>>>(d_partials, grid, d_out);
     return 2;
 }

@@ -9,9 +9,9 @@
 // every round hands its two field elements to a callback, which absorbs them
 // and returns the next challenge, so a Rust prover keeps its own
 // ProverState.  The product layers, the fold of each round by the previous
-// challenge and the round sums run on the GPU; per round the host reads 32
-// bytes (the two reduced sums), multiplies them by the running eq factor,
-// and calls the transcript.
+// challenge and the round sums run on the GPU; per round the kernel's last
+// CTA posts the two reduced sums to mapped host memory, and the host
+// multiplies them by the running eq factor and calls the transcript.
 #include <cuda_runtime.h>
 
 #include <string.h>
@@ -112,7 +112,6 @@ int gkr_run(bz_ctx *ctx, uint4 *d_leaves, size_t n, size_t groups, const uint64_
         p[S - 1 - i].w[1] = point[2 * i + 1];
     }
     Gf claim;
-    uint64_t h_msg[4];
     for (int j = layers - 1; j >= 0; --j) {
         const int k = L - j - 1;  // coordinates of this layer's point
         uint4 *l = layer[j], *r = layer[j] + ((size_t)1 << k);
@@ -136,17 +135,19 @@ int gkr_run(bz_ctx *ctx, uint4 *d_leaves, size_t n, size_t groups, const uint64_
                 const int remaining = k - 1 - rnd;
                 const size_t h = (size_t)1 << remaining;
                 const Gf &z = p[rnd];
+                // the round's last CTA posts the two sums to the mapped
+                // mailbox: no finish kernel, copy or stream synchronisation
+                const MsgPost post = next_msg_post(ctx);
                 ctx->launches += launch_gkr_round(l, r, w, h, pending, to_u4(rho), gzero(z),
                                                   remaining ? w_next : nullptr, d_partials,
-                                                  d_msg, st, ctx->num_sms);
+                                                  d_msg, st, ctx->num_sms, &post);
                 BZ_CUDA(ctx, cudaGetLastError());
-                BZ_CUDA(ctx, cudaMemcpyAsync(h_msg, d_msg, 32, cudaMemcpyDeviceToHost, st));
-                BZ_CUDA(ctx, cudaStreamSynchronize(st));
                 Gf se, si;
-                se.w[0] = h_msg[0];
-                se.w[1] = h_msg[1];
-                si.w[0] = h_msg[2];
-                si.w[1] = h_msg[3];
+                rc = msg_wait(ctx, post.seq_val, se.w, si.w);
+                if (rc) {
+                    reset_msg_ticket(ctx);
+                    return rc;
+                }
                 se = gmul(factor, se);
                 si = gmul(factor, si);
                 const uint64_t msg[4] = {se.w[0], se.w[1], si.w[0], si.w[1]};

@@ -848,6 +848,8 @@ static MsgPost next_post(bz_ctx *ctx) {
     return p;
 }
 
+MsgPost next_msg_post(bz_ctx *ctx) { return next_post(ctx); }
+
 void reset_msg_ticket(bz_ctx *ctx) {
     cudaMemsetAsync((uint8_t *)ctx->d_small + 768, 0, 4, ctx->stream);
 }

@@ -150,4 +150,7 @@ int msg_wait(bz_ctx *ctx, uint32_t seq, uint64_t u0[2], uint64_t u2[2]);
 int mapped_wait(bz_ctx *ctx, size_t offset, uint32_t seq, const char *what);
 // Zero the message ticket (after a round that may have stopped part-way).
 void reset_msg_ticket(bz_ctx *ctx);
+// The mailbox post for the next message kernel on the context stream (its
+// sequence number is what msg_wait then waits for).
+MsgPost next_msg_post(bz_ctx *ctx);
 }  // namespace bz
