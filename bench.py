@@ -570,9 +570,12 @@ def run_gpu(args, ws, rank, local):
 
 def _bench_batch(ctx, bz, L, _lib, args):
     """64 polynomials, log2 sizes uniform on [16, 24] (seed 3), square-ish
-    2^floor(n/2) x 2^ceil(n/2) matrices, rate 1/4: one CUDA-graph launch of a
-    batch plan (per-shape autotuned schedules, 4 parallel branches) against the
-    same 64 committed one at a time by the plain GPU path."""
+    2^floor(n/2) x 2^ceil(n/2) matrices, rate 1/4, per-shape autotuned
+    schedules: the persistent plan (every commit as work items of one
+    persistent kernel, launched through a CUDA graph), the graph plan (every
+    commit's kernels in one CUDA graph over 4 parallel branches) and the same
+    plan issued as stream launches, against the same 64 committed one at a
+    time by the plain GPU path."""
     import numpy as np
 
     rng = np.random.default_rng(3)
@@ -584,8 +587,10 @@ def _bench_batch(ctx, bz, L, _lib, args):
     total = int(sum(1 << n for n in sizes))
     reps = 5
     res = {}
-    for mode, graph, branches in (("graph", True, 4), ("stream_plan", False, 4)):
-        plan = bz.BatchPlan(msgs, params, use_graph=graph, n_branches=branches, ctx=ctx)
+    for mode, graph, branches in (("persistent", True, 0), ("graph", True, 4),
+                                  ("stream_plan", False, 4)):
+        plan = bz.BatchPlan(msgs, params, use_graph=graph, n_branches=branches, ctx=ctx,
+                            persistent=mode == "persistent")
         plan.launch()
         plan.roots()
         ctx.synchronize()
@@ -596,6 +601,8 @@ def _bench_batch(ctx, bz, L, _lib, args):
         roots = plan.roots()
         plan.close()
         res[mode] = {"value": total / (ms / 1e3), "ms": ms}
+        if mode == "persistent":
+            persistent_roots = roots
     # plain: one commit at a time through bz_commit_device (root read per commit)
     import ctypes
 
@@ -609,6 +616,7 @@ def _bench_batch(ctx, bz, L, _lib, args):
 
     plain_roots = plain_once()
     assert plain_roots == roots, "batched roots differ from one-at-a-time roots"
+    assert plain_roots == persistent_roots, "persistent roots differ from one-at-a-time roots"
     ctx.synchronize()
     ctx.timer_begin()
     for _ in range(reps):
@@ -618,7 +626,8 @@ def _bench_batch(ctx, bz, L, _lib, args):
     for m in msgs:
         m.free()
     return {"polys": 64, "total_elems": total, "unit": UNIT, "log2_sizes": sizes,
-            "speedup_graph_vs_plain": res["plain"]["ms"] / res["graph"]["ms"], **res}
+            "speedup_graph_vs_plain": res["plain"]["ms"] / res["graph"]["ms"],
+            "speedup_persistent_vs_plain": res["plain"]["ms"] / res["persistent"]["ms"], **res}
 
 
 def _bench_shapes(ctx, bz):

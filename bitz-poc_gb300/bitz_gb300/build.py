@@ -20,7 +20,7 @@ INCLUDE = os.path.join(os.path.dirname(ROOT), "include")
 
 SOURCES = ["ntt.cu", "merkle.cu", "fold.cu", "runtime.cu", "batch.cu", "serve.cu", "pipeline.cu", "noalloc.cu",
            "transcript.cu", "pow.cu", "open.cu", "codec.cpp", "ligerito.cu",
-           "pcs_open.cu", "ingest.cu", "shard.cu", "gkr.cu"]
+           "pcs_open.cu", "ingest.cu", "shard.cu", "gkr.cu", "persist.cu"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 FLAGS = ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "-Xcompiler", "-O2",
          "--expt-relaxed-constexpr"]

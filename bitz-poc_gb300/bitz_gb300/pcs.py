@@ -402,16 +402,21 @@ def chacha_words(seed: int, n: int, first_word: int = 0, n_threads: int = 0) -> 
 class BatchPlan:
     """Reusable batched commit (bz_batch_plan_*): resident buffers for every
     polynomial and, with ``use_graph``, one CUDA graph holding all kernels,
-    spread over ``n_branches`` parallel branches."""
+    spread over ``n_branches`` parallel branches.  With ``persistent`` every
+    commit runs as work items of one persistent kernel
+    (bz_batch_plan_create_persistent), launched through a CUDA graph."""
 
     def __init__(self, msgs, params_list, use_graph: bool = True, n_branches: int = 4,
-                 ctx: Context | None = None):
+                 ctx: Context | None = None, persistent: bool = False):
         self.ctx = ctx or default_context()
         L = lib()
         for name, res, args in (
                 ("bz_batch_plan_create", ctypes.c_int,
                  [ctypes.c_void_p, ctypes.c_size_t, ctypes.c_void_p, ctypes.POINTER(Params),
                   ctypes.c_int, ctypes.c_int, ctypes.POINTER(ctypes.c_void_p)]),
+                ("bz_batch_plan_create_persistent", ctypes.c_int,
+                 [ctypes.c_void_p, ctypes.c_size_t, ctypes.c_void_p, ctypes.POINTER(Params),
+                  ctypes.POINTER(ctypes.c_void_p)]),
                 ("bz_batch_plan_launch", ctypes.c_int, [ctypes.c_void_p]),
                 ("bz_batch_plan_roots", ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p]),
                 ("bz_batch_plan_commitment", ctypes.c_void_p, [ctypes.c_void_p, ctypes.c_size_t]),
@@ -426,9 +431,13 @@ class BatchPlan:
                                            for m in msgs])
         ps = (Params * self.n)(*[p.to_c() for p in self.params])
         h = ctypes.c_void_p()
-        check(self.ctx.handle, L.bz_batch_plan_create(self.ctx.handle, self.n, arr, ps,
-                                                      1 if use_graph else 0, n_branches,
-                                                      ctypes.byref(h)))
+        if persistent:
+            check(self.ctx.handle, L.bz_batch_plan_create_persistent(
+                self.ctx.handle, self.n, arr, ps, ctypes.byref(h)))
+        else:
+            check(self.ctx.handle, L.bz_batch_plan_create(self.ctx.handle, self.n, arr, ps,
+                                                          1 if use_graph else 0, n_branches,
+                                                          ctypes.byref(h)))
         self.h = h
         self.ctx.adopt(self)
 

@@ -274,21 +274,6 @@ int bz_autotune(bz_ctx *ctx, const bz_params *params, int reps, uint32_t *chosen
 // ===========================================================================
 // Reusable batch plans.
 // ===========================================================================
-struct bz_batch_plan {
-    bz_ctx *ctx = nullptr;
-    std::vector<bz::Shape> shapes;
-    std::vector<const uint4 *> msgs;
-    std::vector<bz_commitment *> commits;
-    std::vector<uint32_t> schedules;
-    uint8_t *d_roots = nullptr;
-    int use_graph = 0;
-    int n_branches = 1;
-    std::vector<cudaStream_t> branches;
-    std::vector<cudaEvent_t> fork_join;  // [0] fork, [1..n] joins
-    cudaGraph_t graph = nullptr;
-    cudaGraphExec_t exec = nullptr;
-};
-
 namespace {
 
 // Enqueue every commit of the plan: polynomials are dealt to the branch
@@ -336,6 +321,7 @@ int bz_batch_plan_destroy(bz_batch_plan *p) {
     for (auto *c : p->commits)
         if (c) bz_commitment_free(c);
     if (p->d_roots) dev_free(ctx, p->d_roots, 0, false);
+    if (p->d_persist) dev_free(ctx, p->d_persist, 0, false);
     for (auto s : p->branches) cudaStreamDestroy(s);
     for (auto e : p->fork_join) cudaEventDestroy(e);
     cudaStreamSynchronize(ctx->stream);
@@ -425,7 +411,9 @@ int bz_batch_plan_launch(bz_batch_plan *p) {
     if (p->use_graph) {
         cudaError_t e = cudaGraphLaunch(p->exec, ctx->stream);
         if (e != cudaSuccess) return set_err(ctx, BZ_ERR_CUDA, "graph launch", e);
-        ctx->launches += 0;  // kernel count recorded at capture time
+        // a graph of per-commit kernels was counted at capture time; a
+        // persistent plan's graph holds one kernel
+        if (p->d_persist) ctx->launches += 1;
         return BZ_OK;
     }
     return plan_enqueue(p);
@@ -436,8 +424,14 @@ int bz_batch_plan_roots(bz_batch_plan *p, uint8_t *roots) {
     bz_ctx *ctx = p->ctx;
     const size_t n = p->commits.size();
     cudaError_t e = cudaMemcpyAsync(roots, p->d_roots, n * 32, cudaMemcpyDeviceToHost, ctx->stream);
+    uint32_t perr = 0;
+    if (e == cudaSuccess && p->d_persist_err)
+        e = cudaMemcpyAsync(&perr, p->d_persist_err, 4, cudaMemcpyDeviceToHost, ctx->stream);
     if (e == cudaSuccess) e = cudaStreamSynchronize(ctx->stream);
     if (e != cudaSuccess) return set_err(ctx, BZ_ERR_CUDA, "plan roots", e);
+    if (perr)
+        return set_msg(ctx, BZ_ERR_TIMEOUT,
+                       "persistent batch: a CTA found no ready work item within its limit");
     for (size_t i = 0; i < n; ++i) {
         memcpy(p->commits[i]->root, roots + 32 * i, 32);
         p->commits[i]->root_ready = true;

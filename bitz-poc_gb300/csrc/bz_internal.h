@@ -86,6 +86,8 @@ int launch_table_pass(const Shape &s, int layer, int layers, const uint4 *src, i
                       cudaStream_t st, int num_sms, uint32_t schedule);
 // Bit length of the widest twiddle of `layer` in the ell-layer transform.
 int twiddle_bits(int ell, int layer);
+// Shapes whose whole transform runs in one ntt_small_kernel launch.
+bool small_ntt_ok(const Shape &s);
 int launch_deep_range(const Shape &s, int deep, int mode, const uint4 *src, int src_bits,
                       uint4 *dst, const uint4 *tw, uint64_t p0, uint64_t p1, cudaStream_t st,
                       int num_sms);

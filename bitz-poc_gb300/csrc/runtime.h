@@ -13,6 +13,7 @@
 #include <mutex>
 #include <set>
 #include <string>
+#include <vector>
 
 #include "../../include/bitz_gpu.h"
 #include "bz_internal.h"
@@ -72,6 +73,26 @@ struct bz_ctx {
     std::thread side_thread;
     bool side_stop = false;
     uint64_t root_ring = 0;              // next 32-byte slot of h_small for async roots
+};
+
+// A reusable batch plan (batch.cu; the persistent form is built in persist.cu).
+struct bz_batch_plan {
+    bz_ctx *ctx = nullptr;
+    std::vector<bz::Shape> shapes;
+    std::vector<const uint4 *> msgs;
+    std::vector<bz_commitment *> commits;
+    std::vector<uint32_t> schedules;
+    uint8_t *d_roots = nullptr;
+    int use_graph = 0;
+    int n_branches = 1;
+    std::vector<cudaStream_t> branches;
+    std::vector<cudaEvent_t> fork_join;  // [0] fork, [1..n] joins
+    cudaGraph_t graph = nullptr;
+    cudaGraphExec_t exec = nullptr;
+    // persistent plans: one device block holding the steps, the commit table
+    // and the scheduler state; the graph resets the state and runs the kernel
+    void *d_persist = nullptr;
+    uint32_t *d_persist_err = nullptr;  // nonzero after a CTA gave up waiting
 };
 
 // Return BZ_ERR_CUDA (recording the failing call) when a CUDA call fails.

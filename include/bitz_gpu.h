@@ -204,6 +204,20 @@ typedef struct bz_batch_plan bz_batch_plan;
 int bz_batch_plan_create(bz_ctx *ctx, size_t count, const uint64_t *const *d_msgs,
                          const bz_params *params, int use_graph, int n_branches,
                          bz_batch_plan **out);
+/* The same resident commits run as the work items of ONE persistent kernel
+ * (one 512-thread CTA per SM), launched through a CUDA graph together with the
+ * reset of its scheduler state.  Every commit's NTT passes, leaf hashes and
+ * tree levels are steps of items; a CTA takes an item of the first commit
+ * (largest first) whose current step still has one, so small commits fill the
+ * SMs while a large one finishes a step.  The context's per-shape schedules
+ * (bz_autotune) pick the radix-8, radix-4 / radix-2 and deep passes; shapes
+ * too small for the table passes take generic single layers.  BZ_ERR_SHAPE
+ * for single-column messages and BLAKE3 leaves of more than 256 chunks
+ * (2^14 lanes).  A CTA that finds no ready item for 2 s stops, and
+ * bz_batch_plan_roots then returns BZ_ERR_TIMEOUT.  Launch, roots,
+ * commitment and destroy are those of any plan. */
+int bz_batch_plan_create_persistent(bz_ctx *ctx, size_t count, const uint64_t *const *d_msgs,
+                                    const bz_params *params, bz_batch_plan **out);
 /* Enqueue one launch of the plan on the context stream (no synchronization). */
 int bz_batch_plan_launch(bz_batch_plan *plan);
 /* Synchronize and copy the count roots (count * 32 bytes). */
