@@ -141,9 +141,13 @@ __device__ bool claim_item(const PersistArgs &p, int &g_out, uint32_t &idx_out) 
 
 // Each item kind runs in a function of its own (not inlined), so every body
 // gets the registers it has as a standalone kernel instead of sharing one
-// allocation across all of them.
+// allocation across all of them.  The functions address the dynamic shared
+// memory through this array, not through a pointer argument, so the compiler
+// keeps the tables' addresses as 32-bit shared-window offsets.
+extern __shared__ uint4 persist_smem[];
 template <int A, int B, int C>
-__device__ __noinline__ void pass8_item(const PStep *st, uint64_t b, uint64_t e, char *base) {
+__device__ __noinline__ void pass8_item(const PStep *st, uint64_t b, uint64_t e) {
+    char *base = reinterpret_cast<char *>(persist_smem);
     const TablePassArgs a = st->tp;
     uint4 *twb = reinterpret_cast<uint4 *>(base + kPass8Smem);
     uint64_t *win = reinterpret_cast<uint64_t *>(twb + kTw8Window * 7);
@@ -151,7 +155,8 @@ __device__ __noinline__ void pass8_item(const PStep *st, uint64_t b, uint64_t e,
 }
 
 template <int O, int AB>
-__device__ __noinline__ void pf_item(const PStep *st, uint64_t b, uint64_t e, char *base) {
+__device__ __noinline__ void pf_item(const PStep *st, uint64_t b, uint64_t e) {
+    char *base = reinterpret_cast<char *>(persist_smem);
     const TablePassArgs a = st->tp;
     uint4 *twb = reinterpret_cast<uint4 *>(base + pf_smem(O, AB));
     uint64_t *win = reinterpret_cast<uint64_t *>(twb + kTwWindow * 3);
@@ -159,7 +164,8 @@ __device__ __noinline__ void pf_item(const PStep *st, uint64_t b, uint64_t e, ch
 }
 
 template <int LAYERS>
-__device__ __noinline__ void tp_item(const PStep *st, uint64_t b, uint64_t e, char *base) {
+__device__ __noinline__ void tp_item(const PStep *st, uint64_t b, uint64_t e) {
+    char *base = reinterpret_cast<char *>(persist_smem);
     const TablePassArgs a = st->tp;
     uint4 *twb = reinterpret_cast<uint4 *>(base + table_smem(LAYERS));
     uint64_t *win = reinterpret_cast<uint64_t *>(twb + kTwWindow * (LAYERS == 2 ? 3 : 1));
@@ -179,7 +185,8 @@ __device__ __noinline__ void generic_item(const PStep *st, uint64_t b, uint64_t 
                        b + threadIdx.x, e, blockDim.x);
 }
 
-__device__ __noinline__ void leaves_item(const PStep *st, uint64_t b, uint64_t e, char *base) {
+__device__ __noinline__ void leaves_item(const PStep *st, uint64_t b, uint64_t e) {
+    char *base = reinterpret_cast<char *>(persist_smem);
     const uint4 *cw = st->cw;
     uint32_t *leaves = st->leaves;
     if (st->kind == PK_B3_CHUNKED) {
@@ -197,7 +204,8 @@ __device__ __noinline__ void leaves_item(const PStep *st, uint64_t b, uint64_t e
     }
 }
 
-__device__ __noinline__ void levels_item(const PStep *st, uint64_t b, uint64_t e, char *base) {
+__device__ __noinline__ void levels_item(const PStep *st, uint64_t b, uint64_t e) {
+    char *base = reinterpret_cast<char *>(persist_smem);
     const LevelsArgs a = st->lv;
     uint32_t(*nodes)[9] = reinterpret_cast<uint32_t(*)[9]>(base);
     for (uint64_t u = b; u < e; ++u) {
@@ -206,16 +214,15 @@ __device__ __noinline__ void levels_item(const PStep *st, uint64_t b, uint64_t e
     }
 }
 
-__device__ __forceinline__ void run_item(const PStep *st, uint32_t idx, uint4 *dsm) {
+__device__ __forceinline__ void run_item(const PStep *st, uint32_t idx) {
     const uint64_t units = st->units, n = st->n_items;
     const uint64_t b = units * idx / n, e = units * (idx + 1) / n;
-    char *base = reinterpret_cast<char *>(dsm);
     const int v = st->variant;
     switch (st->kind) {
         case PK_PASS8:
             switch (v) {
 #define BZ_P8(A, B, C) \
-    case A * 100 + B * 10 + C: pass8_item<A, B, C>(st, b, e, base); break;
+    case A * 100 + B * 10 + C: pass8_item<A, B, C>(st, b, e); break;
                 BZ_P8(4, 4, 4) BZ_P8(4, 4, 2) BZ_P8(4, 4, 1) BZ_P8(4, 2, 2) BZ_P8(4, 2, 1)
                 BZ_P8(4, 1, 1) BZ_P8(2, 2, 2) BZ_P8(2, 2, 1) BZ_P8(2, 1, 1) BZ_P8(1, 1, 1)
 #undef BZ_P8
@@ -225,15 +232,15 @@ __device__ __forceinline__ void run_item(const PStep *st, uint32_t idx, uint4 *d
         case PK_PF:
             switch (v) {
 #define BZ_PF(O, AB) \
-    case O * 10 + AB: pf_item<O, AB>(st, b, e, base); break;
+    case O * 10 + AB: pf_item<O, AB>(st, b, e); break;
                 BZ_PF(4, 4) BZ_PF(4, 2) BZ_PF(4, 1) BZ_PF(2, 2) BZ_PF(2, 1) BZ_PF(1, 1)
 #undef BZ_PF
                 default: break;
             }
             break;
         case PK_TP:
-            if (v == 2) tp_item<2>(st, b, e, base);
-            else tp_item<1>(st, b, e, base);
+            if (v == 2) tp_item<2>(st, b, e);
+            else tp_item<1>(st, b, e);
             break;
         case PK_DEEP:
             if (v == 1) deep_item<1>(st, b, e);
@@ -244,8 +251,8 @@ __device__ __forceinline__ void run_item(const PStep *st, uint32_t idx, uint4 *d
         case PK_GENERIC: generic_item(st, b, e); break;
         case PK_B3_CHUNKED:
         case PK_B3_SMALL:
-        case PK_SHA: leaves_item(st, b, e, base); break;
-        case PK_LEVELS: levels_item(st, b, e, base); break;
+        case PK_SHA: leaves_item(st, b, e); break;
+        case PK_LEVELS: levels_item(st, b, e); break;
         default: break;
     }
 }
@@ -269,7 +276,6 @@ __device__ void finish_item(const PersistArgs &p, int g) {
 }
 
 __global__ void __launch_bounds__(512, 1) persistent_batch_kernel(PersistArgs p) {
-    extern __shared__ uint4 dsm[];
     __shared__ int s_g;
     __shared__ uint32_t s_idx;
     for (;;) {
@@ -301,7 +307,7 @@ __global__ void __launch_bounds__(512, 1) persistent_batch_kernel(PersistArgs p)
         const int g = s_g;
         const uint32_t idx = s_idx;
         if (g < 0) return;
-        run_item(p.steps + g, idx, dsm);
+        run_item(p.steps + g, idx);
         __syncthreads();
         if (threadIdx.x == 0) finish_item(p, g);
     }
