@@ -18,10 +18,13 @@
 // Scheduling: queued commits are admitted smallest first, except that a
 // request that has waited longer than the aging bound goes first (so a large
 // request is never starved), or in arrival order (bz_server_set_policy).
-// Half the slots run high-priority streams and take requests of at most 2^20
-// elements (and openings); large requests take the other half, whose table
-// passes run as short CTAs, so a small request's kernels get SMs within a
-// fraction of a large commit's pass.  A small request's message is read from
+// The slots' streams have three priorities: a third of them the highest, for
+// small requests of at most 2^small_log elements (2^20 by default) and for
+// openings; a third a middle one, for medium requests of at most
+// 2^(small_log + 3) elements; the rest the lowest, for the largest.  A request
+// takes a slot of its own tier or, when those are busy, of a lower one, never a
+// higher one.  Medium and large requests' table passes run as short CTAs, so a
+// higher tier's kernels get SMs within a fraction of their pass.  A small request's message is read from
 // pinned host memory by a copy kernel, so it never queues behind a large
 // upload on the copy engine.  A commit-then-open
 // request enqueues its opening (row gather, multi-proof nodes, the copies to
@@ -99,13 +102,14 @@ struct bz_server {
     int n_slots = 0;
     uint64_t budget = 0, in_use = 0;
     size_t queue_cap = 0;
-    // one stream per slot: the first n_hi slots have high priority and serve
-    // small requests (and openings), the others serve large ones (and small
-    // ones when every high slot is busy).  One stream per slot keeps the
-    // streams within the device's hardware work queues, so no two slots'
-    // kernels serialise behind each other.
+    // one stream per slot: the first n_hi slots have the highest priority and
+    // serve small requests (and openings), the next n_mid a middle priority
+    // for medium requests, the rest the lowest for the largest; a request may
+    // also take a slot of a lower tier than its own.  One stream per slot
+    // keeps the streams within the device's hardware work queues, so no two
+    // slots' kernels serialise behind each other.
     std::vector<cudaStream_t> streams;
-    int n_hi = 0;
+    int n_hi = 0, n_mid = 0;
     std::vector<cudaEvent_t> slot_done;    // completion of the slot's work
     std::vector<uint8_t *> slot_host;      // pinned staging (root, rows, nodes)
     std::vector<size_t> slot_host_bytes;
@@ -204,6 +208,14 @@ int ensure_slot_host(bz_server *S, int slot, size_t bytes) {
 #endif
 
 bool is_large(const bz_server *S, const Shape &s) { return s.log_msg_len > S->small_log; }
+
+// Priority tier of a request: 0 small, 1 medium, 2 the largest (everything
+// tier 0 when priorities are off).
+constexpr int kMidSpan = 3;  // medium: up to 2^(small_log + kMidSpan) elements
+int tier_of(const bz_server *S, const Shape &s) {
+    if (S->small_log < 0 || s.log_msg_len <= S->small_log) return 0;
+    return s.log_msg_len <= S->small_log + kMidSpan ? 1 : 2;
+}
 
 // Wakes the scheduler once a slot's work is done (runs on a CUDA callback
 // thread: no CUDA call and no lock here; the scheduler's wait has a short
@@ -374,37 +386,35 @@ void free_commit_buffers(bz_server *S, Request *r, int slot) {
     }
 }
 
-// High-priority slots while small requests have priority: half of them.
-int hi_slots(const bz_server *S) { return S->small_log >= 0 ? S->n_hi : 0; }
+// First slot of a tier (slots of tiers t, t+1, .. follow it); every slot when
+// priorities are off.  With too few slots for three tiers the lower tiers
+// share the last slot.
+int tier_first_slot(const bz_server *S, int tier) {
+    if (S->small_log < 0 || tier == 0) return 0;
+    return std::min(S->n_slots - 1, tier == 1 ? S->n_hi : S->n_hi + S->n_mid);
+}
 
-// A free slot for a request (-1: none): large requests take the
-// normal-priority slots only, small ones (and openings) prefer the
-// high-priority ones.
-int free_slot(bz_server *S, bool large) {
-    const int h = hi_slots(S);
-    if (!large)
-        for (int i = 0; i < h; ++i)
-            if (!S->slot_busy[i]) return i;
-    for (int i = h; i < S->n_slots; ++i)
+// A free slot for a request of the given tier (-1: none): its own tier's
+// slots first, then those of lower priority.
+int free_slot(bz_server *S, int tier) {
+    for (int i = tier_first_slot(S, tier); i < S->n_slots; ++i)
         if (!S->slot_busy[i]) return i;
     return -1;
 }
 
 // The next queued commit to admit and its slot ({0, -1}: none now): the
 // oldest when it has waited past the aging bound (or in arrival order), else
-// the smallest; a large request with no free normal-priority slot gives way
-// to the smallest small one.
+// the smallest; a request with no free slot in its tier or below gives way to
+// the smallest queued one.
 std::pair<uint64_t, int> next_commit(bz_server *S) {
     const uint64_t oldest = *S->pend_by_id.begin();
     uint64_t id = oldest;
     if (S->admit_order == BZ_ADMIT_SMALLEST && S->ns() - S->reqs[oldest]->t_submit <= S->aging_ns)
         id = S->pend_by_size.begin()->second;
-    bool large = is_large(S, S->reqs[id]->shape);
-    int slot = free_slot(S, large);
-    if (slot < 0 && large) {
+    int slot = free_slot(S, tier_of(S, S->reqs[id]->shape));
+    if (slot < 0) {
         id = S->pend_by_size.begin()->second;
-        large = is_large(S, S->reqs[id]->shape);
-        slot = large ? -1 : free_slot(S, false);
+        slot = free_slot(S, tier_of(S, S->reqs[id]->shape));
     }
     return slot < 0 ? std::make_pair((uint64_t)0, -1) : std::make_pair(id, slot);
 }
@@ -473,7 +483,7 @@ void scheduler(bz_server *S) {
         }
         // 2. openings first (they free memory)
         while (!S->pending_opens.empty()) {
-            const int slot = free_slot(S, false);
+            const int slot = free_slot(S, 0);
             if (slot < 0) break;
             Request *r = S->reqs[S->pending_opens.front()].get();
             S->pending_opens.pop_front();
@@ -546,7 +556,8 @@ int bz_server_create(bz_ctx *ctx, int n_slots, uint64_t mem_budget_bytes, size_t
     S->budget = mem_budget_bytes ? mem_budget_bytes : ctx->budget;
     S->queue_cap = queue_cap ? queue_cap : 1 << 20;
     S->streams.assign(n_slots, nullptr);
-    S->n_hi = n_slots / 2;
+    S->n_hi = std::max(1, n_slots / 3);
+    S->n_mid = (n_slots - S->n_hi) / 2;
     S->slot_done.assign(n_slots, nullptr);
     S->slot_host.assign(n_slots, nullptr);
     S->slot_host_bytes.assign(n_slots, 0);
@@ -570,7 +581,9 @@ int bz_server_create(bz_ctx *ctx, int n_slots, uint64_t mem_budget_bytes, size_t
     }
     for (int i = 0; i < n_slots; ++i) {
         if (cudaStreamCreateWithPriority(&S->streams[i], cudaStreamNonBlocking,
-                                         i < S->n_hi ? greatest : least) != cudaSuccess ||
+                                         i < S->n_hi ? greatest
+                                         : i < S->n_hi + S->n_mid ? (greatest + least) / 2
+                                                                  : least) != cudaSuccess ||
             cudaEventCreateWithFlags(&S->slot_done[i], cudaEventDisableTiming) != cudaSuccess ||
             ensure_slot_host(S, i, 1 << 20) != BZ_OK) {
             cudaGetLastError();

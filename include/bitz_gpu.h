@@ -250,12 +250,15 @@ int bz_server_create(bz_ctx *ctx, int n_slots, uint64_t mem_budget_bytes, size_t
 /* Scheduling policy (no counterpart in the reference, which has no server).
  * admit_order: BZ_ADMIT_SMALLEST (the default) admits the smallest queued
  * commit first, unless the oldest has waited more than aging_ms (default 500),
- * which then goes first; BZ_ADMIT_FIFO admits in arrival order.  Requests of
+ * which then goes first; BZ_ADMIT_FIFO admits in arrival order.  The slots'
+ * streams have three priorities (a third each, the rest lowest): requests of
  * at most 2^high_priority_log_size elements (default 20; -1: no priorities)
- * run on the high-priority half of the slots (and on the other half when
- * those are busy); larger requests run on the other half only, their table
- * passes cut into short CTAs, so a small request's kernels take SMs within a
- * fraction of a large commit's pass.  A commit-then-open request's opening
+ * and openings take the highest, medium requests of at most
+ * 2^(high_priority_log_size + 3) elements the middle one, the largest the
+ * lowest.  A request also takes a slot of a lower priority than its own when
+ * its own are busy, never a higher one; medium and large requests' table
+ * passes are cut into short CTAs, so a higher-priority request's kernels take
+ * SMs within a fraction of their pass.  A commit-then-open request's opening
  * always runs right behind its commit on the same stream. */
 enum { BZ_ADMIT_FIFO = 0, BZ_ADMIT_SMALLEST = 1 };
 int bz_server_set_policy(bz_server *s, int admit_order, uint32_t aging_ms,
