@@ -27,6 +27,7 @@
 #include <cuda_runtime.h>
 
 #include <algorithm>
+#include <cstring>
 #include <numeric>
 #include <string>
 #include <vector>
@@ -626,6 +627,9 @@ extern "C" int bz_batch_plan_create_persistent(bz_ctx *ctx, size_t count,
         if (e != cudaSuccess) rc = set_err(ctx, BZ_ERR_CUDA, "persistent plan setup", e);
         else if (per_sm < 1) rc = set_msg(ctx, BZ_ERR_CUDA, "persistent batch kernel does not fit an SM");
         if (rc == BZ_OK) {
+            p->persist_args.assign(reinterpret_cast<const char *>(&args),
+                                   reinterpret_cast<const char *>(&args) + sizeof args);
+            p->persist_state_bytes = state_bytes;
             // one graph: reset the scheduler state, then the kernel
             e = cudaStreamBeginCapture(ctx->stream, cudaStreamCaptureModeThreadLocal);
             if (e == cudaSuccess) {
@@ -648,4 +652,33 @@ extern "C" int bz_batch_plan_create_persistent(bz_ctx *ctx, size_t count,
     }
     *out = p;
     return BZ_OK;
+}
+
+// Test hook: one direct launch of the plan's kernel that expects one step more
+// than the plan has, with a wait limit of limit_ms.  Every CTA runs the real
+// items, then finds nothing ready and gives up after the limit; the error word
+// is read back and the state reset.  BZ_ERR_TIMEOUT when the kernel reported
+// the expired wait.
+extern "C" int bz_batch_plan_stall_check(bz_batch_plan *p, uint32_t limit_ms) {
+    if (!p || p->persist_args.size() != sizeof(PersistArgs) || limit_ms == 0) return BZ_ERR_ARG;
+    bz_ctx *ctx = p->ctx;
+    PersistArgs args;
+    memcpy(&args, p->persist_args.data(), sizeof args);
+    args.total_steps += 1;  // a step that no item completes
+    args.limit_ns = (uint64_t)limit_ms * 1000000ull;
+    uint32_t *state = args.steps_done;
+    uint32_t err = 0;
+    cudaError_t e = cudaMemsetAsync(state, 0, p->persist_state_bytes, ctx->stream);
+    if (e == cudaSuccess) {
+        persistent_batch_kernel<<<ctx->num_sms, 512, kPersistSmem, ctx->stream>>>(args);
+        e = cudaGetLastError();
+    }
+    if (e == cudaSuccess)
+        e = cudaMemcpyAsync(&err, args.err, 4, cudaMemcpyDeviceToHost, ctx->stream);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(ctx->stream);
+    if (e == cudaSuccess) e = cudaMemsetAsync(state, 0, p->persist_state_bytes, ctx->stream);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(ctx->stream);
+    if (e != cudaSuccess) return set_err(ctx, BZ_ERR_CUDA, "persistent stall check", e);
+    return err ? set_msg(ctx, BZ_ERR_TIMEOUT, "persistent batch: bounded wait ran out")
+               : BZ_OK;
 }

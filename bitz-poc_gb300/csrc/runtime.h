@@ -93,6 +93,8 @@ struct bz_batch_plan {
     // and the scheduler state; the graph resets the state and runs the kernel
     void *d_persist = nullptr;
     uint32_t *d_persist_err = nullptr;  // nonzero after a CTA gave up waiting
+    std::vector<char> persist_args;      // the kernel's arguments (relaunch by the stall check)
+    size_t persist_state_bytes = 0;
 };
 
 // Return BZ_ERR_CUDA (recording the failing call) when a CUDA call fails.

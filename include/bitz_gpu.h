@@ -218,6 +218,12 @@ int bz_batch_plan_create(bz_ctx *ctx, size_t count, const uint64_t *const *d_msg
  * commitment and destroy are those of any plan. */
 int bz_batch_plan_create_persistent(bz_ctx *ctx, size_t count, const uint64_t *const *d_msgs,
                                     const bz_params *params, bz_batch_plan **out);
+/* Test hook for a persistent plan (no counterpart in the reference): one
+ * launch that waits for a step the plan does not have, with a wait limit of
+ * limit_ms.  The kernel runs the plan's items, gives up waiting after the
+ * limit and reports it; returns BZ_ERR_TIMEOUT when it did (the plan's later
+ * launches are unaffected), BZ_ERR_ARG for a plan that is not persistent. */
+int bz_batch_plan_stall_check(bz_batch_plan *plan, uint32_t limit_ms);
 /* Enqueue one launch of the plan on the context stream (no synchronization). */
 int bz_batch_plan_launch(bz_batch_plan *plan);
 /* Synchronize and copy the count roots (count * 32 bytes). */

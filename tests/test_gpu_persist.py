@@ -145,3 +145,34 @@ def test_persistent_plan_single_commit_2e22(ctx):
     finally:
         plan.close()
         m.free()
+
+
+def test_persistent_plan_bounded_wait_reports_and_recovers(ctx):
+    """A launch that waits for a step no item completes: every CTA gives up
+    after the 30 ms limit, the host reads BZ_ERR_TIMEOUT, and the plan's next
+    launches still give the single commits' roots."""
+    import ctypes
+
+    from bitz_gb300 import BatchPlan, DeviceArray, PcsParams, _lib, commit
+
+    L = _lib.lib()
+    L.bz_batch_plan_stall_check.restype = ctypes.c_int
+    L.bz_batch_plan_stall_check.argtypes = [ctypes.c_void_p, ctypes.c_uint32]
+    params = [PcsParams(18 + 7, 2, 9, 1), PcsParams(14 + 7, 2, 7, 1)]
+    msgs = [DeviceArray.chacha(900 + i, 1 << (p.m - 7), ctx) for i, p in enumerate(params)]
+    plan = BatchPlan(msgs, params, ctx=ctx, persistent=True)
+    graph_plan = BatchPlan(msgs, params, ctx=ctx)
+    try:
+        assert L.bz_batch_plan_stall_check(plan.h, 30) == 6          # BZ_ERR_TIMEOUT
+        assert L.bz_batch_plan_stall_check(graph_plan.h, 30) == 1    # not persistent
+        plan.launch()
+        roots = plan.roots()
+        for m, p, r in zip(msgs, params, roots):
+            c, pd = commit(m, p, ctx)
+            pd.free()
+            assert r == c.root
+    finally:
+        plan.close()
+        graph_plan.close()
+        for m in msgs:
+            m.free()
