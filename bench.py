@@ -24,6 +24,13 @@ import time
 
 import numpy as np
 
+# One hardware work queue per stream (CUDA's default is 8 per device, read once
+# before the process's first CUDA call): the server's slot streams, the batch
+# plan's branches and the context's own streams would otherwise share queues,
+# and a small request's kernels could wait behind a large one's in the same
+# queue whatever their stream priorities.
+os.environ.setdefault("CUDA_DEVICE_MAX_CONNECTIONS", "32")
+
 REPO = os.path.dirname(os.path.abspath(__file__))
 for _p in (REPO, os.path.join(REPO, "bitz-poc_gb300")):
     if _p not in sys.path:
