@@ -73,7 +73,7 @@ def test_oracle_chacha_matches_fixture(oracle):
 def test_pcs_params_geometry():
     from bitz_gb300 import PcsParams, HashKind
 
-    # BASELINE shapes: 2^a x 2^b, rate 1/4 -> m = a + b + 7
+    # benchmark shapes: 2^a x 2^b, rate 1/4 -> m = a + b + 7
     for a, b in [(10, 10), (12, 12), (14, 14)]:
         p = PcsParams(a + b + 7, 2, a, HashKind.BLAKE3)
         assert p.k_code() == b + 2
