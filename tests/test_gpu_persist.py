@@ -176,3 +176,38 @@ def test_persistent_plan_bounded_wait_reports_and_recovers(ctx):
         graph_plan.close()
         for m in msgs:
             m.free()
+
+
+@pytest.mark.parametrize("persistent", [True, False])
+def test_plan_recommits_changed_messages(oracle, ctx, persistent):
+    """A plan recommits its device messages at every launch: after the
+    messages are overwritten in place, the next launch's roots are the new
+    messages' (the persistent kernel's scheduler state restarts each launch)."""
+    import ctypes
+
+    from bitz_gb300 import BatchPlan, DeviceArray, PcsParams, _lib
+
+    L = _lib.lib()
+    shapes = [(16, 2, 8), (18, 2, 9)]
+    params = [PcsParams(lm + 7, r, lb, 1) for (lm, r, lb) in shapes]
+    msgs = [DeviceArray.from_host(oracle.chacha_words(40 + i, 1 << lm), ctx)
+            for i, (lm, _, _) in enumerate(shapes)]
+    plan = BatchPlan(msgs, params, ctx=ctx, persistent=persistent)
+    try:
+        plan.launch()
+        first = plan.roots()
+        for seed in (50, 60):
+            new = [oracle.chacha_words(seed + i, 1 << lm) for i, (lm, _, _) in enumerate(shapes)]
+            for m, h in zip(msgs, new):
+                _lib.check(ctx.handle, L.bz_memcpy_h2d(ctx.handle, ctypes.c_void_p(m.ptr.value),
+                                                       h.ctypes.data_as(ctypes.c_void_p),
+                                                       h.nbytes))
+            plan.launch()
+            roots = plan.roots()
+            for i, (lm, r, lb) in enumerate(shapes):
+                assert roots[i] == oracle.commit(new[i], r, lb, 1, n_threads=8)[2]
+                assert roots[i] != first[i]
+    finally:
+        plan.close()
+        for m in msgs:
+            m.free()
