@@ -24,9 +24,10 @@
 // 2^(small_log + 3) elements; the rest the lowest, for the largest.  A request
 // takes a slot of its own tier or, when those are busy, of a lower one, never a
 // higher one.  Medium and large requests' table passes run as short CTAs, so a
-// higher tier's kernels get SMs within a fraction of their pass.  A small request's message is read from
-// pinned host memory by a copy kernel, so it never queues behind a large
-// upload on the copy engine.  A commit-then-open
+// higher tier's kernels get SMs within a fraction of their pass.  A small or
+// medium request's message is read from pinned host memory by a copy kernel,
+// so it never queues behind a large upload on the copy engine; the largest
+// requests' uploads go to the copy engine in 64 MiB pieces.  A commit-then-open
 // request enqueues its opening (row gather, multi-proof nodes, the copies to
 // the slot's pinned staging) right behind its commit on the same stream: one
 // completion, no second trip through the scheduler.  Each slot's work ends
@@ -317,12 +318,15 @@ int start_commit(bz_server *S, Request *r, int slot) {
         return BZ_ERR_NOMEM;
     }
     r->commit = c;
-    // A small request's message is read from pinned host memory by a copy
-    // kernel on its high-priority stream (as fast as the copy engine, both
-    // being limited by the host link), so it never waits on the copy engine
-    // behind a large request's upload.  Large and pageable messages go
-    // through the copy engine.
-    const void *dev_view = large ? nullptr : mapped_view(r->host_msg);
+    // A small or medium request's message is read from pinned host memory by
+    // a copy kernel on its own stream (as fast as the copy engine, both being
+    // limited by the host link), so it never waits on the copy engine behind
+    // a large request's upload: through the copy engine, 2^21-2^23 requests
+    // waited 15-80 ms behind the 0.5-1 GiB uploads of the largest.  The
+    // largest tier's and pageable messages go through the copy engine, in
+    // pieces that let the other streams' copies in between.
+    const bool ce_upload = S->small_log < 0 || tier_of(S, s) == 2;
+    const void *dev_view = ce_upload ? nullptr : mapped_view(r->host_msg);
     if (dev_view) {
         const uint64_t n = s.msg_words();
         const unsigned grid = (unsigned)std::max<uint64_t>(
@@ -330,7 +334,11 @@ int start_commit(bz_server *S, Request *r, int slot) {
         upload_kernel<<<grid, 256, 0, st>>>(static_cast<const uint4 *>(dev_view), r->d_msg, n);
         ctx->launches += 1;
     } else {
-        cudaMemcpyAsync(r->d_msg, r->host_msg, s.msg_words() * 16, cudaMemcpyHostToDevice, st);
+        const size_t total = s.msg_words() * 16, piece = (size_t)64 << 20;
+        for (size_t off = 0; off < total; off += piece)
+            cudaMemcpyAsync(reinterpret_cast<uint8_t *>(r->d_msg) + off,
+                            reinterpret_cast<const uint8_t *>(r->host_msg) + off,
+                            std::min(piece, total - off), cudaMemcpyHostToDevice, st);
     }
     const uint4 *d_tw = nullptr;
     int rc = get_twiddles(ctx, s.k_code(), &d_tw);
