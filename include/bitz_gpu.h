@@ -269,9 +269,11 @@ int bz_server_create(bz_ctx *ctx, int n_slots, uint64_t mem_budget_bytes, size_t
 enum { BZ_ADMIT_FIFO = 0, BZ_ADMIT_SMALLEST = 1 };
 int bz_server_set_policy(bz_server *s, int admit_order, uint32_t aging_ms,
                          int high_priority_log_size);
-/* host_msg must stay valid until the request reaches BZ_REQ_COMMITTED
- * (pinned host memory gives overlapped copies).  BZ_ERR_BUSY when the queue
- * holds queue_cap commits. */
+/* host_msg must stay valid until the request reaches BZ_REQ_COMMITTED.
+ * From pinned host memory, small and medium messages are read by a copy
+ * kernel on the request's stream and the largest go through the copy engine
+ * in 64 MiB pieces; a pageable message always takes the copy engine.
+ * BZ_ERR_BUSY when the queue holds queue_cap commits. */
 int bz_server_submit_commit(bz_server *s, const uint64_t *host_msg, size_t n_words,
                             const bz_params *params, uint64_t *request_id);
 /* Commit-then-open as one request: the opening at the q positions runs right
