@@ -34,8 +34,9 @@
 // with a host callback that wakes the scheduler.
 //
 // Nothing on the request path synchronises the device: device buffers come
-// from the server's stream-ordered pool (cudaMallocFromPoolAsync / cudaFreeAsync on the slot's
-// stream), and each slot owns its completion event and a grow-only pinned
+// from the buffers of finished requests of the same size or else from the
+// server's stream-ordered pool (cudaMallocFromPoolAsync / cudaFreeAsync on
+// the slot's stream), and each slot owns its completion event and a grow-only pinned
 // staging buffer for the root, rows and proof nodes, which the scheduler
 // copies into the request when the slot's work completes.  A completion
 // queue (bz_server_next_done) hands state changes to the caller without
@@ -133,6 +134,14 @@ struct bz_server {
     // allocation could take memory a large request freed and be made to wait
     // for that request's stream.
     cudaMemPool_t pool = nullptr;
+    // Device buffers of finished requests, by size, kept for the next request
+    // of the same size (sizes are powers of two, so a few recur).  Taking
+    // them does not block: a pool allocation that has to map more memory holds
+    // the scheduler (and every completion behind it) for 5-7 ms at a 2^26
+    // request, and the pool had to whenever its free blocks were too small
+    // for the request or not yet known complete on another stream.
+    std::map<size_t, std::vector<void *>> spare;
+    uint64_t spare_bytes = 0;
     std::map<uint64_t, std::unique_ptr<Request>> reqs;
     std::vector<uint64_t> running;  // commit or open in flight
     uint64_t next_id = 1;
@@ -287,6 +296,50 @@ size_t open_staging_bytes(const Request *r) {
     return r->positions.size() * r->shape.leaf_bytes() + r->node_idx.size() * 32;
 }
 
+// Spare buffers back to the pool (their work is complete), freed in st's order.
+void drop_spares(bz_server *S, cudaStream_t st) {
+    for (auto &kv : S->spare)
+        for (void *p : kv.second) cudaFreeAsync(p, st);
+    S->spare.clear();
+    S->spare_bytes = 0;
+}
+
+// A device buffer of the given size for work on st: a spare one if any, else
+// one from the pool (after giving the spares back to it when the pool alone
+// cannot serve the size).  Null when the device is out of memory.
+void *take_buffer(bz_server *S, size_t bytes, cudaStream_t st) {
+    auto it = S->spare.find(bytes);
+    if (it != S->spare.end() && !it->second.empty()) {
+        void *p = it->second.back();
+        it->second.pop_back();
+        S->spare_bytes -= bytes;
+        return p;
+    }
+    // the live requests (this one included) and the spares stay within the budget
+    if (S->in_use + S->spare_bytes > S->budget) drop_spares(S, st);
+    void *p = nullptr;
+    if (cudaMallocFromPoolAsync(&p, bytes, S->pool, st) == cudaSuccess) return p;
+    cudaGetLastError();
+    if (S->spare_bytes == 0) return nullptr;
+    drop_spares(S, st);
+    if (cudaMallocFromPoolAsync(&p, bytes, S->pool, st) == cudaSuccess) return p;
+    cudaGetLastError();
+    return nullptr;
+}
+
+// A buffer whose work is complete (its slot's event was seen): kept as a spare
+// while the live requests and the spares fit in the budget, else back to the
+// pool.
+void give_buffer(bz_server *S, void *p, size_t bytes, cudaStream_t st) {
+    if (!p) return;
+    if (S->in_use + S->spare_bytes + bytes <= S->budget) {
+        S->spare[bytes].push_back(p);
+        S->spare_bytes += bytes;
+    } else {
+        cudaFreeAsync(p, st);
+    }
+}
+
 // Start a commit on a free slot (caller holds the lock).  A commit-then-open
 // request's opening follows on the same stream; the root lands in the first
 // 32 bytes of the slot's staging, the opening's rows and nodes after it.
@@ -299,18 +352,17 @@ int start_commit(bz_server *S, Request *r, int slot) {
         const int rc = ensure_slot_host(S, slot, 32 + open_staging_bytes(r));
         if (rc) return rc;
     }
-    cudaError_t e = cudaMallocFromPoolAsync((void **)&r->d_msg, s.msg_words() * 16, S->pool, st);
-    if (e != cudaSuccess) return BZ_ERR_NOMEM;
+    r->d_msg = static_cast<uint4 *>(take_buffer(S, s.msg_words() * 16, st));
+    if (!r->d_msg) return BZ_ERR_NOMEM;
     bz_commitment *c = new bz_commitment();
     c->ctx = ctx;
     c->shape = s;
     c->cw_bytes = s.cw_words() * 16;
     c->tree_bytes = s.tree_nodes() * 32;
-    e = cudaMallocFromPoolAsync((void **)&c->d_cw, c->cw_bytes, S->pool, st);
-    if (e == cudaSuccess)
-        e = cudaMallocFromPoolAsync((void **)&c->d_tree, c->tree_bytes, S->pool, st);
-    if (e != cudaSuccess) {
-        cudaGetLastError();
+    c->d_cw = static_cast<uint4 *>(take_buffer(S, c->cw_bytes, st));
+    if (c->d_cw) c->d_tree = static_cast<uint8_t *>(take_buffer(S, c->tree_bytes, st));
+    if (!c->d_cw || !c->d_tree) {
+        // nothing has used them yet: freed in st's order
         if (c->d_cw) cudaFreeAsync(c->d_cw, st);
         cudaFreeAsync(r->d_msg, st);
         r->d_msg = nullptr;
@@ -355,8 +407,6 @@ int start_commit(bz_server *S, Request *r, int slot) {
     int n = launch_commit_kernels(ctx, s, schedule, r->d_msg, c->d_cw, c->d_tree, d_tw, st,
                                   nullptr);
     ctx->launches += (uint64_t)n;
-    cudaFreeAsync(r->d_msg, st);
-    r->d_msg = nullptr;
     cudaMemcpyAsync(S->slot_host[slot], c->d_tree + (s.tree_nodes() - 1) * 32, 32,
                     cudaMemcpyDeviceToHost, st);
     r->fused_open = false;
@@ -367,9 +417,7 @@ int start_commit(bz_server *S, Request *r, int slot) {
     }
     cudaEventRecord(S->slot_done[slot], st);
     cudaLaunchHostFunc(st, slot_done_cb, S);
-    e = cudaGetLastError();
-    if (e != cudaSuccess) return BZ_ERR_CUDA;
-    return BZ_OK;
+    return cudaGetLastError() == cudaSuccess ? BZ_OK : BZ_ERR_CUDA;
 }
 
 int start_open(bz_server *S, Request *r, int slot) {
@@ -383,12 +431,19 @@ int start_open(bz_server *S, Request *r, int slot) {
     return cudaGetLastError() == cudaSuccess ? BZ_OK : BZ_ERR_CUDA;
 }
 
-void free_commit_buffers(bz_server *S, Request *r, int slot) {
+// The codeword and tree of r.  complete: the slot's work on them is known
+// complete (its event was seen), so they may become spares; otherwise (a
+// failed request) they go back to the pool in the stream's order.
+void free_commit_buffers(bz_server *S, Request *r, int slot, bool complete) {
     if (r->commit) {
-        // the slot's work on these buffers is complete (its event was seen)
         cudaStream_t st = S->streams[slot >= 0 ? slot : 0];
-        cudaFreeAsync(r->commit->d_cw, st);
-        cudaFreeAsync(r->commit->d_tree, st);
+        if (complete) {
+            give_buffer(S, r->commit->d_cw, r->commit->cw_bytes, st);
+            give_buffer(S, r->commit->d_tree, r->commit->tree_bytes, st);
+        } else {
+            cudaFreeAsync(r->commit->d_cw, st);
+            cudaFreeAsync(r->commit->d_tree, st);
+        }
         delete r->commit;
         r->commit = nullptr;
     }
@@ -453,12 +508,17 @@ void scheduler(bz_server *S) {
                                 src + q_rows * row_words * 8 + nn * 32);
                 r->state = RS_OPENED;
                 r->t_opened = S->ns();
-                free_commit_buffers(S, r, r->slot);
                 S->in_use -= r->bytes - r->shape.msg_words() * 16;
+                free_commit_buffers(S, r, r->slot, true);
                 ++S->n_opened;
             };
             if (q != cudaSuccess) {
                 cudaGetLastError();
+                if (r->d_msg) {  // a failed commit: its message buffer goes back to the pool
+                    cudaFreeAsync(r->d_msg, S->streams[r->slot]);
+                    r->d_msg = nullptr;
+                    S->in_use -= r->shape.msg_words() * 16;
+                }
                 r->state = RS_FAILED;
                 r->error = BZ_ERR_CUDA;
                 ++S->n_failed;
@@ -468,7 +528,9 @@ void scheduler(bz_server *S) {
                 memcpy(r->commit->root, r->root, 32);
                 r->state = RS_COMMITTED;
                 r->t_committed = S->ns();
-                S->in_use -= r->shape.msg_words() * 16;  // staging buffer released
+                S->in_use -= r->shape.msg_words() * 16;  // the message buffer is free
+                give_buffer(S, r->d_msg, r->shape.msg_words() * 16, S->streams[r->slot]);
+                r->d_msg = nullptr;
                 ++S->n_committed;
                 if (r->fused_open) {
                     // the opening ran behind the commit on the same stream
@@ -526,6 +588,10 @@ void scheduler(bz_server *S) {
             r->t_start = S->ns();
             const int rc = start_commit(S, r, slot);
             if (rc) {
+                // whatever it allocated goes back to the pool behind what it enqueued
+                free_commit_buffers(S, r, slot, false);
+                if (r->d_msg) cudaFreeAsync(r->d_msg, S->streams[slot]);
+                r->d_msg = nullptr;
                 r->state = RS_FAILED;
                 r->error = rc;
                 S->in_use -= r->bytes;
@@ -783,7 +849,7 @@ int bz_server_release(bz_server *S, uint64_t id) {
     Request *r = it->second.get();
     if (r->state != RS_OPENED && r->state != RS_FAILED) return BZ_ERR_STATE;
     if (r->state == RS_FAILED && r->commit) {
-        free_commit_buffers(S, r, r->slot);
+        free_commit_buffers(S, r, r->slot, false);
         S->in_use -= r->bytes - r->shape.msg_words() * 16;
     }
     S->reqs.erase(it);
@@ -813,8 +879,10 @@ int bz_server_destroy(bz_server *S) {
     for (auto s : S->streams) cudaStreamSynchronize(s);
     for (auto &kv : S->reqs) {
         Request *r = kv.second.get();
-        if (r->commit) free_commit_buffers(S, r, 0);
+        if (r->commit) free_commit_buffers(S, r, 0, false);
+        if (r->d_msg) cudaFreeAsync(r->d_msg, S->streams[0]);
     }
+    drop_spares(S, S->streams[0]);
     for (auto s : S->streams) {
         cudaStreamSynchronize(s);
         cudaStreamDestroy(s);
