@@ -238,7 +238,10 @@ int bz_batch_plan_destroy(bz_batch_plan *plan);
  * staging + resident codeword + tree) fits in mem_budget_bytes (0 = the
  * context budget); later arrivals start as earlier ones finish or are opened,
  * and their kernels overlap on the device.  Codewords and trees stay resident
- * until opened.  The serving counterpart of the reference's
+ * until opened.  A finished request's device buffers are kept for the next
+ * request of the same size while the live requests and these spares fit in
+ * the budget; bz_server_stats's in_use counts the live requests only, and
+ * bz_server_destroy returns everything.  The serving counterpart of the reference's
  * commit-then-open flow (BinaryPcs::commit then open_*, src/binary_pcs.rs:
  * 313-431); the reference has no server of its own. */
 typedef struct bz_server bz_server;
