@@ -66,7 +66,7 @@ enum : uint32_t {
     SCHED_NARROW = 0x4000,        // compact 32-bit tables for the deepest layers' twiddles
     SCHED_RADIX8 = 0x8000,        // radix-8 passes (eight 32 KB byte tables per twiddle)
     SCHED_R8_HEAD = 0x10000,      // with SCHED_RADIX8: the 1-2 leftover layers run first
-    SCHED_SHORT_CTAS = 0x200000,  // table passes in 8 CTAs per SM instead of one long one
+    SCHED_SHORT_CTAS = 0x200000,  // table passes in 16 CTAs per SM instead of one long one
 };
 uint32_t default_schedule(const Shape &s);
 
